@@ -1,0 +1,452 @@
+// C ABI of liballium_sweep.so (declared in include/allium_sweep.h).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+struct allium_sweep {
+    allium::Handle h;
+};
+
+using allium::Handle;
+
+namespace {
+
+#define CUDA_OR_FAIL(h, x)                                   \
+    do {                                                     \
+        cudaError_t _e = (x);                                \
+        if (_e != cudaSuccess) {                             \
+            (h).last_error = std::string(#x) + ": " + cudaGetErrorString(_e); \
+            return ALLIUM_ERR_CUDA;                          \
+        }                                                    \
+    } while (0)
+
+bool on_device(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+cudaError_t ensure(T** buf, size_t count) {
+    if (*buf) return cudaSuccess;
+    return cudaMalloc(buf, count * sizeof(T));
+}
+
+// device copy of a small input array (host or device pointer)
+template <typename T>
+int upload(Handle& h, const T* src, size_t count, T** dst) {
+    CUDA_OR_FAIL(h, ensure(dst, count));
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyDefault, h.stream));
+    return ALLIUM_OK;
+}
+
+int check_status(Handle& h) {
+    int st = 0;
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(&st, h.d_status, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    if (st) {
+        CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_status, 0, sizeof(int), h.stream));
+        if (st & allium::kErrSingular) { h.last_error = "zero pivot in a local solve"; return ALLIUM_ERR_SINGULAR; }
+        h.last_error = "non-finite value";
+        return ALLIUM_ERR_NAN;
+    }
+    return ALLIUM_OK;
+}
+
+void free_all(Handle& h) {
+    void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
+                    h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
+                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
+}
+
+int refresh_fp32(Handle& h) {
+    if (!h.fp32_ready) return ALLIUM_OK;
+    CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
+    return ALLIUM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* allium_status_string(int s) {
+    switch (s) {
+        case ALLIUM_OK: return "ok";
+        case ALLIUM_ERR_ARG: return "invalid argument";
+        case ALLIUM_ERR_NOT_DAG: return "upwind graph is not a DAG";
+        case ALLIUM_ERR_SIZE: return "size mismatch";
+        case ALLIUM_ERR_TIMEOUT: return "device wait timed out";
+        case ALLIUM_ERR_NAN: return "non-finite value";
+        case ALLIUM_ERR_CUDA: return "CUDA error";
+        case ALLIUM_ERR_UNSUPPORTED: return "unsupported option";
+        case ALLIUM_ERR_MESH: return "malformed mesh";
+        case ALLIUM_ERR_SINGULAR: return "singular local system";
+        default: return "unknown status";
+    }
+}
+
+const char* allium_sweep_last_error(const allium_sweep* s) { return s ? s->h.last_error.c_str() : "null handle"; }
+
+int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, const allium_quad_desc* quad,
+                        int num_groups, const double* sigma_t, const allium_bc_desc* bc, allium_sweep** out) {
+    if (!out) return ALLIUM_ERR_ARG;
+    *out = nullptr;
+    if (!mesh || !fe || !quad || !sigma_t || num_groups < 1) return ALLIUM_ERR_ARG;
+    if (mesh->dim < 1 || mesh->dim > 3 || quad->dim != mesh->dim || mesh->num_elements < 1 ||
+        !mesh->vertices || !mesh->element_vertices || quad->num_angles < 1 || !quad->omega || !quad->weights)
+        return ALLIUM_ERR_ARG;
+    if (fe->order < 0 || fe->order > allium::kMaxOrder || fe->basis != ALLIUM_BASIS_GAUSS_LOBATTO ||
+        fe->lump < 0 || fe->lump > 7)
+        return ALLIUM_ERR_UNSUPPORTED;
+    if (mesh->dim == 3 && fe->order > 1) return ALLIUM_ERR_UNSUPPORTED;
+    if (bc)
+        for (int i = 0; i < bc->num; ++i)
+            if (bc->kinds[i] != ALLIUM_BC_INFLOW) return ALLIUM_ERR_UNSUPPORTED;
+
+    allium_sweep* s = new allium_sweep;
+    Handle& h = s->h;
+    h.dim = mesh->dim; h.p = fe->order; h.lump = fe->lump;
+    h.ne = mesh->num_elements; h.Nw = quad->num_angles; h.G = num_groups;
+    h.ref = allium::make_ref_tables(h.dim, h.p, h.lump);
+    h.n = h.ref.n; h.nf = h.ref.nf; h.nface = h.ref.nface;
+    h.ndof = (long long)h.ne * h.n;
+    h.psi_size = (long long)h.G * h.Nw * h.ndof;
+    h.h_omega.assign(quad->omega, quad->omega + (size_t)h.Nw * h.dim);
+    h.h_weights.assign(quad->weights, quad->weights + h.Nw);
+    h.wsum = 0.0;
+    for (double w : h.h_weights) h.wsum += w;
+
+    auto fail = [&](int st) {
+        free_all(h);
+        std::fprintf(stderr, "allium_sweep_create: %s (%s)\n", allium_status_string(st), h.last_error.c_str());
+        delete s;
+        return st;
+    };
+
+    allium::Topology topo;
+    int st = allium::build_topology(*mesh, h.p, topo, h.last_error);
+    if (st != ALLIUM_OK) return fail(st);
+    h.nfaces = topo.nfaces;
+
+    if (cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        h.last_error = "cannot create a CUDA stream (no device?)";
+        return fail(ALLIUM_ERR_CUDA);
+    }
+    h.own_stream = true;
+    const long long N = (long long)h.ne * h.Nw;
+    const size_t nn = (size_t)h.n * h.n;
+#define STEP(x) do { int _s = (x); if (_s != ALLIUM_OK) return fail(_s); } while (0)
+#define CSTEP(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { h.last_error = std::string(#x) + ": " + cudaGetErrorString(_e); return fail(ALLIUM_ERR_CUDA); } } while (0)
+    STEP(upload(h, h.h_omega.data(), h.h_omega.size(), &h.d_omega));
+    STEP(upload(h, h.h_weights.data(), h.h_weights.size(), &h.d_weights));
+    STEP(upload(h, topo.corners.data(), topo.corners.size(), &h.d_corners));
+    STEP(upload(h, topo.slots.data(), topo.slots.size(), &h.d_slots));
+    STEP(upload(h, topo.face_e1k1.data(), topo.face_e1k1.size(), &h.d_face_e1k1));
+    STEP(upload(h, topo.nbrmap.data(), topo.nbrmap.size(), &h.d_nbrmap));
+    STEP(upload(h, sigma_t, (size_t)h.G * h.ne, &h.d_sigma));
+    CSTEP(cudaMalloc(&h.d_normals, (size_t)h.nfaces * h.dim * sizeof(double)));
+    CSTEP(cudaMalloc(&h.d_G, (size_t)h.ne * h.dim * nn * sizeof(double)));
+    CSTEP(cudaMalloc(&h.d_M, (size_t)h.ne * nn * sizeof(double)));
+    CSTEP(cudaMalloc(&h.d_F, (size_t)h.ne * h.nface * h.nf * h.nf * sizeof(double)));
+    CSTEP(cudaMalloc(&h.d_level, N * sizeof(int)));
+    CSTEP(cudaMalloc(&h.d_level_nodes, N * sizeof(int)));
+    CSTEP(cudaMalloc(&h.d_status, sizeof(int)));
+    CSTEP(cudaMemsetAsync(h.d_status, 0, sizeof(int), h.stream));
+    h.scratch_len = 4096;
+    CSTEP(cudaMalloc(&h.d_scratch, (h.scratch_len + 1) * sizeof(double)));
+    CSTEP(allium::launch_face_normals(h));
+    CSTEP(allium::launch_assemble(h));
+    STEP(allium::compute_levels(h));
+    CSTEP(cudaStreamSynchronize(h.stream));
+#undef STEP
+#undef CSTEP
+    *out = s;
+    return ALLIUM_OK;
+}
+
+void allium_sweep_destroy(allium_sweep* s) {
+    if (!s) return;
+    if (s->h.stream) cudaStreamSynchronize(s->h.stream);
+    free_all(s->h);
+    delete s;
+}
+
+int allium_sweep_set_stream(allium_sweep* s, void* stream) {
+    if (!s) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!stream) {
+        if (!h.own_stream) {
+            CUDA_OR_FAIL(h, cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+            h.own_stream = true;
+        }
+        return ALLIUM_OK;
+    }
+    if (h.own_stream) {
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+        cudaStreamDestroy(h.stream);
+        h.own_stream = false;
+    }
+    h.stream = (cudaStream_t)stream;
+    return ALLIUM_OK;
+}
+
+int allium_sweep_sizes(const allium_sweep* s, long long* psi_size, long long* num_dofs, int* num_levels) {
+    if (!s) return ALLIUM_ERR_ARG;
+    if (psi_size) *psi_size = s->h.psi_size;
+    if (num_dofs) *num_dofs = s->h.ndof;
+    if (num_levels) *num_levels = s->h.num_levels;
+    return ALLIUM_OK;
+}
+
+int allium_sweep_assemble(allium_sweep* s, const double* sigma_t) {
+    if (!s || !sigma_t) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    int st = upload(h, sigma_t, (size_t)h.G * h.ne, &h.d_sigma);
+    if (st) return st;
+    st = refresh_fp32(h);
+    if (st) return st;
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    return ALLIUM_OK;
+}
+
+static int ensure_mass2(Handle& h) {
+    if (h.have_mass2) return ALLIUM_OK;
+    CUDA_OR_FAIL(h, cudaMalloc(&h.d_Mt, (size_t)h.ne * h.n * h.n * sizeof(double)));
+    CUDA_OR_FAIL(h, allium::launch_time_mass(h));
+    h.have_mass2 = true;
+    return ALLIUM_OK;
+}
+
+int allium_sweep_set_time_absorption(allium_sweep* s, double tau) {
+    if (!s) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    h.tau = tau;
+    if (!h.time_dependent) {
+        int st = ensure_mass2(h);
+        if (st) return st;
+        h.time_dependent = true;
+        st = refresh_fp32(h);
+        if (st) return st;
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    }
+    return ALLIUM_OK;
+}
+
+int allium_sweep_scattering_source(allium_sweep* s, const double* sigma_s, const double* phi,
+                                   const double* q_fixed, double* out) {
+    if (!s || !sigma_s || !phi || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    int st = ensure_mass2(h);
+    if (st) return st;
+    const size_t pbytes = (size_t)h.psi_size * sizeof(double);
+    const size_t mbytes = (size_t)h.G * h.ndof * sizeof(double);
+    double *dsig = nullptr, *dphi = nullptr, *dq = nullptr;
+    st = upload(h, sigma_s, (size_t)h.G * h.ne, &dsig);
+    const bool dph = on_device(phi), dqf = q_fixed && on_device(q_fixed), dout = on_device(out);
+    cudaError_t e = cudaSuccess;
+    const double* xp = phi;
+    const double* xq = q_fixed;
+    double* y = out;
+    if (!st && !dph) { e = cudaMalloc(&dphi, mbytes); if (e == cudaSuccess) e = cudaMemcpyAsync(dphi, phi, mbytes, cudaMemcpyHostToDevice, h.stream); xp = dphi; }
+    if (!st && e == cudaSuccess && q_fixed && !dqf) { e = cudaMalloc(&dq, pbytes); if (e == cudaSuccess) e = cudaMemcpyAsync(dq, q_fixed, pbytes, cudaMemcpyHostToDevice, h.stream); xq = dq; }
+    if (!st && e == cudaSuccess && !dout) { e = ensure(&h.d_stage, (size_t)h.psi_size); y = h.d_stage; }
+    if (!st && e == cudaSuccess) e = allium::launch_scatter_source(h, dsig, xp, xq, y);
+    if (!st && e == cudaSuccess && !dout) e = cudaMemcpyAsync(out, y, pbytes, cudaMemcpyDeviceToHost, h.stream);
+    if (!st && e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    if (dsig) cudaFree(dsig);
+    if (dphi) cudaFree(dphi);
+    if (dq) cudaFree(dq);
+    if (st) return st;
+    CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_mult(allium_sweep* s, const double* source, double* psi) {
+    if (!s || !source || !psi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    const bool ds = on_device(source), dp = on_device(psi);
+    if (ds && dp) {
+        CUDA_OR_FAIL(h, allium::launch_sweep_fp64(h, source, psi));
+        return ALLIUM_OK;
+    }
+    CUDA_OR_FAIL(h, ensure(&h.d_stage, (size_t)h.psi_size));
+    const size_t bytes = (size_t)h.psi_size * sizeof(double);
+    const double* src = source;
+    if (!ds) {
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(h.d_stage, source, bytes, cudaMemcpyHostToDevice, h.stream));
+        src = h.d_stage;
+    }
+    double* out = dp ? psi : h.d_stage;
+    CUDA_OR_FAIL(h, allium::launch_sweep_fp64(h, src, out));
+    if (!dp) CUDA_OR_FAIL(h, cudaMemcpyAsync(psi, h.d_stage, bytes, cudaMemcpyDeviceToHost, h.stream));
+    return check_status(h);
+}
+
+int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi) {
+    if (!s || !source || !psi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
+    const bool ds = on_device(source), dp = on_device(psi);
+    if (ds && dp) {
+        CUDA_OR_FAIL(h, allium::launch_sweep_fp32(h, source, psi));
+        return ALLIUM_OK;
+    }
+    CUDA_OR_FAIL(h, ensure(&h.f_stage, (size_t)h.psi_size));
+    const size_t bytes = (size_t)h.psi_size * sizeof(float);
+    const float* src = source;
+    if (!ds) {
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(h.f_stage, source, bytes, cudaMemcpyHostToDevice, h.stream));
+        src = h.f_stage;
+    }
+    float* out = dp ? psi : h.f_stage;
+    CUDA_OR_FAIL(h, allium::launch_sweep_fp32(h, src, out));
+    if (!dp) CUDA_OR_FAIL(h, cudaMemcpyAsync(psi, h.f_stage, bytes, cudaMemcpyDeviceToHost, h.stream));
+    return check_status(h);
+}
+
+int allium_sweep_apply_L(allium_sweep* s, const double* x, double* y) {
+    if (!s || !x || !y) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if ((const void*)x == (const void*)y) { h.last_error = "apply_L needs distinct x and y"; return ALLIUM_ERR_ARG; }
+    const bool dx = on_device(x), dy = on_device(y);
+    if (dx && dy) {
+        CUDA_OR_FAIL(h, allium::launch_apply_L_fp64(h, x, y));
+        return ALLIUM_OK;
+    }
+    const size_t bytes = (size_t)h.psi_size * sizeof(double);
+    double *bx = nullptr, *by = nullptr;
+    if (!dx) {
+        CUDA_OR_FAIL(h, ensure(&h.d_stage, (size_t)h.psi_size));
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(h.d_stage, x, bytes, cudaMemcpyHostToDevice, h.stream));
+        bx = h.d_stage;
+    }
+    if (!dy) CUDA_OR_FAIL(h, cudaMalloc(&by, bytes));
+    cudaError_t e = allium::launch_apply_L_fp64(h, dx ? x : bx, dy ? y : by);
+    if (e == cudaSuccess && !dy) e = cudaMemcpyAsync(y, by, bytes, cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    if (by) cudaFree(by);
+    CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_balance(allium_sweep* s, const double* psi, double* out) {
+    if (!s || !psi || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    const double* x = psi;
+    if (!on_device(psi)) {
+        CUDA_OR_FAIL(h, ensure(&h.d_stage, (size_t)h.psi_size));
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(h.d_stage, psi, (size_t)h.psi_size * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+        x = h.d_stage;
+    }
+    int nb = 0;
+    CUDA_OR_FAIL(h, allium::launch_balance(h, x, h.d_scratch, (int)h.scratch_len, &nb));
+    double* res = h.d_scratch + h.scratch_len;
+    CUDA_OR_FAIL(h, allium::launch_balance_finish(h, h.d_scratch, nb, res));
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(out, res, sizeof(double), cudaMemcpyDefault, h.stream));
+    if (!on_device(out)) CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_moments(allium_sweep* s, const double* psi, double* phi, int nmom) {
+    if (!s || !psi || !phi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (nmom != 1 && nmom != h.dim + 1) return ALLIUM_ERR_ARG;
+    const bool dps = on_device(psi), dph = on_device(phi);
+    const size_t pbytes = (size_t)h.psi_size * sizeof(double);
+    const size_t mbytes = (size_t)h.G * nmom * h.ndof * sizeof(double);
+    const double* x = psi;
+    if (!dps) {
+        CUDA_OR_FAIL(h, ensure(&h.d_stage, (size_t)h.psi_size));
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(h.d_stage, psi, pbytes, cudaMemcpyHostToDevice, h.stream));
+        x = h.d_stage;
+    }
+    double* y = phi;
+    if (!dph) CUDA_OR_FAIL(h, cudaMalloc(&y, mbytes));
+    cudaError_t e = allium::launch_moments(h, x, y, nmom);
+    if (e == cudaSuccess && !dph) e = cudaMemcpyAsync(phi, y, mbytes, cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess && (!dph || !dps)) e = cudaStreamSynchronize(h.stream);
+    if (!dph) cudaFree(y);
+    CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_moments_transpose(allium_sweep* s, const double* phi, double* psi, int nmom, double alpha, int add) {
+    if (!s || !psi || !phi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (nmom != 1 && nmom != h.dim + 1) return ALLIUM_ERR_ARG;
+    const bool dps = on_device(psi), dph = on_device(phi);
+    const size_t pbytes = (size_t)h.psi_size * sizeof(double);
+    const size_t mbytes = (size_t)h.G * nmom * h.ndof * sizeof(double);
+    const double* x = phi;
+    double* tmp = nullptr;
+    if (!dph) {
+        CUDA_OR_FAIL(h, cudaMalloc(&tmp, mbytes));
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(tmp, phi, mbytes, cudaMemcpyHostToDevice, h.stream));
+        x = tmp;
+    }
+    double* y = psi;
+    cudaError_t e = cudaSuccess;
+    if (!dps) {
+        e = ensure(&h.d_stage, (size_t)h.psi_size);
+        if (e == cudaSuccess && add) e = cudaMemcpyAsync(h.d_stage, psi, pbytes, cudaMemcpyHostToDevice, h.stream);
+        y = h.d_stage;
+    }
+    if (e == cudaSuccess) e = allium::launch_moments_transpose(h, x, y, nmom, alpha, add);
+    if (e == cudaSuccess && !dps) e = cudaMemcpyAsync(psi, y, pbytes, cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess && (!dps || !dph)) e = cudaStreamSynchronize(h.stream);
+    if (tmp) cudaFree(tmp);
+    CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow, int num_attr, double* source) {
+    if (!s || !source || (inflow && num_attr < 1)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    double *dq = nullptr, *di = nullptr;
+    int st = ALLIUM_OK;
+    if (q_cell) st = upload(h, q_cell, (size_t)h.G * h.ne, &dq);
+    if (!st && inflow) st = upload(h, inflow, (size_t)h.G * num_attr, &di);
+    if (st) { if (dq) cudaFree(dq); if (di) cudaFree(di); return st; }
+    const bool dsrc = on_device(source);
+    double* out = source;
+    cudaError_t e = cudaSuccess;
+    if (!dsrc) {
+        e = ensure(&h.d_stage, (size_t)h.psi_size);
+        out = h.d_stage;
+    }
+    if (e == cudaSuccess) e = allium::launch_form_source(h, dq, di, inflow ? num_attr : 0, out);
+    if (e == cudaSuccess && !dsrc)
+        e = cudaMemcpyAsync(source, out, (size_t)h.psi_size * sizeof(double), cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    if (dq) cudaFree(dq);
+    if (di) cudaFree(di);
+    CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_levels(allium_sweep* s, int* levels) {
+    if (!s || !levels) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(levels, h.d_level, (size_t)h.ne * h.Nw * sizeof(int), cudaMemcpyDefault, h.stream));
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_synchronize(allium_sweep* s) {
+    if (!s) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    CUDA_OR_FAIL(h, cudaGetLastError());
+    return check_status(h);
+}
+
+}  // extern "C"

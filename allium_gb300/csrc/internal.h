@@ -1,0 +1,111 @@
+// Internal state of one sweep handle and the kernel launchers shared by the
+// translation units of liballium_sweep.so.  Nothing here is part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/allium_sweep.h"
+
+namespace allium {
+
+constexpr int kMaxOrder = 3;
+constexpr int kMaxRule = 5;   // largest 1D rule used (p + 2 points, p <= 3)
+
+// Reference-element tables, passed to kernels by value.
+struct RefTables {
+    int dim, p, n1, n, nf, nface;
+    double nodes[kMaxOrder + 1];          // Gauss-Lobatto basis nodes on [0,1]
+    // 1D rules: 0 = sigma mass, 1 = convection, 2 = time mass, 3 = face mass,
+    //           4 = source domain, 5 = source boundary
+    int rn[6];
+    double rx[6][kMaxRule], rw[6][kMaxRule];
+};
+
+// Per (cell, local face) topology.  face < 0 never happens; nbr < 0 on the
+// boundary.  side = 0 when the cell is the face's element 1 (lower index).
+struct Slot {
+    int face, nbr, side, attr;
+};
+
+struct SweepArgsBase {
+    int ne, Nw, G, dim;
+    long long ndof;
+    const double* omega;     // [Nw][dim]
+    const double* normals;   // [nfaces][dim] unit, out of element 1
+    const Slot* slots;       // [ne][2 dim]
+    const uint8_t* nbrmap;   // [ne][2 dim][nf] nbr local DOF of each self face DOF
+};
+
+struct Handle {
+    // problem description
+    int dim = 0, p = 0, n = 0, nf = 0, nface = 0, ne = 0, Nw = 0, G = 0, lump = 0;
+    int nfaces = 0;
+    long long ndof = 0, psi_size = 0;
+    RefTables ref{};
+    bool time_dependent = false;
+    bool have_mass2 = false;         // d_Mt assembled (time absorption or scattering)
+    double tau = 0.0;
+    double wsum = 0.0;
+    std::vector<double> h_omega, h_weights;
+    std::vector<int> h_level_offsets;   // [num_levels + 1]
+    int num_levels = 0;
+
+    // device buffers
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    double *d_omega = nullptr, *d_weights = nullptr, *d_corners = nullptr, *d_normals = nullptr;
+    Slot* d_slots = nullptr;
+    int* d_face_e1k1 = nullptr;      // [nfaces][2]
+    uint8_t* d_nbrmap = nullptr;
+    double *d_G = nullptr, *d_M = nullptr, *d_Mt = nullptr, *d_F = nullptr, *d_sigma = nullptr;
+    float *f_G = nullptr, *f_M = nullptr, *f_Mt = nullptr, *f_F = nullptr, *f_sigma = nullptr;
+    int* d_level = nullptr;          // [ne*Nw]
+    int* d_level_nodes = nullptr;    // [ne*Nw] sorted by (level, node)
+    int* d_status = nullptr;         // sticky kernel error bits
+    double* d_stage = nullptr;       // psi-sized staging buffer for host pointers
+    float* f_stage = nullptr;
+    double* d_scratch = nullptr;     // reduction partials
+    size_t scratch_len = 0;
+    bool fp32_ready = false;
+
+    std::string last_error;
+};
+
+// kernel error bits (d_status)
+constexpr int kErrSingular = 1;
+constexpr int kErrNaN = 2;
+
+// ---- topology (topology.cpp, host)
+struct Topology {
+    int nfaces = 0;
+    std::vector<int> face_e1k1;       // [nfaces][2]
+    std::vector<Slot> slots;          // [ne][2 dim]
+    std::vector<uint8_t> nbrmap;      // [ne][2 dim][nf]
+    std::vector<double> corners;      // [ne][2^dim][dim], corner order c = c0 + 2 c1 + 4 c2
+};
+int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string& err);
+
+// ---- setup kernels (setup.cu)
+cudaError_t launch_face_normals(Handle& h);
+cudaError_t launch_assemble(Handle& h);
+cudaError_t launch_time_mass(Handle& h);
+int compute_levels(Handle& h);   // returns an allium status
+cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out);
+cudaError_t launch_moments(Handle& h, const double* psi, double* phi, int nmom);
+cudaError_t launch_moments_transpose(Handle& h, const double* phi, double* psi, int nmom, double alpha, int add);
+cudaError_t launch_balance(Handle& h, const double* psi, double* partial, int nblocks_max, int* nblocks);
+cudaError_t launch_balance_finish(Handle& h, const double* partial, int nparts, double* out);
+cudaError_t launch_scatter_source(Handle& h, const double* sigma_s, const double* phi, const double* qfix, double* out);
+cudaError_t make_fp32_copies(Handle& h);
+RefTables make_ref_tables(int dim, int p, int lump);
+
+// ---- hot kernels (sweep_fp64.cu, sweep_fp32.cu)
+cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi);
+cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi);
+cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y);
+
+}  // namespace allium

@@ -1,0 +1,702 @@
+// Setup-side kernels of the sweep: reference tables, face normals, local
+// matrix assembly (AssembleLocalMatrices), device wavefront levels, the
+// transport source, the moment operators and the balance reduction.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <cmath>
+#include <vector>
+
+#include "geometry.cuh"
+#include "sweep_kernels.cuh"
+
+namespace allium {
+
+// ------------------------------------------------------------ host tables
+namespace {
+
+double legendre_p(int n, double x, double* dp) {
+    double p0 = 1.0, p1 = x;
+    if (n == 0) { *dp = 0.0; return 1.0; }
+    for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+        p0 = p1; p1 = p2;
+    }
+    *dp = n * (x * p1 - p0) / (x * x - 1.0);
+    return p1;
+}
+
+// n-point Gauss-Legendre on [0,1] (Newton on P_n from Chebyshev-like guesses)
+void gauss_legendre01(int n, double* x, double* w) {
+    for (int i = 0; i < (n + 1) / 2; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            const double pz = legendre_p(n, z, &dp);
+            const double dz = pz / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-17) break;
+        }
+        legendre_p(n, z, &dp);
+        const double wt = 1.0 / ((1.0 - z * z) * dp * dp);   // half of the [-1,1] weight
+        x[n - 1 - i] = 0.5 * (1.0 + z);
+        x[i] = 0.5 * (1.0 - z);
+        w[i] = w[n - 1 - i] = wt;
+    }
+    if (n % 2) x[n / 2] = 0.5;
+}
+
+void gauss_lobatto01(int p, double* x) {
+    if (p == 0) { x[0] = 0.5; return; }
+    x[0] = 0.0; x[p] = 1.0;
+    for (int i = 1; i < p; ++i) {
+        double z = -std::cos(M_PI * i / p);
+        for (int it = 0; it < 100; ++it) {
+            double dp = 0.0;
+            const double pp = legendre_p(p, z, &dp);
+            const double d2 = (2.0 * z * dp - p * (p + 1.0) * pp) / (1.0 - z * z);
+            const double dz = dp / d2;
+            z -= dz;
+            if (std::fabs(dz) < 1e-17) break;
+        }
+        x[i] = 0.5 * (1.0 + z);
+    }
+}
+
+void set_rule(RefTables& t, int r, int npts, bool vertex) {
+    if (vertex) {
+        t.rn[r] = 2;
+        t.rx[r][0] = 0.0; t.rx[r][1] = 1.0;
+        t.rw[r][0] = 0.5; t.rw[r][1] = 0.5;
+    } else {
+        t.rn[r] = npts;
+        gauss_legendre01(npts, t.rx[r], t.rw[r]);
+    }
+}
+
+}  // namespace
+
+// Integration rules follow the point counts MFEM's IntRules give the
+// integrators allium uses (n = order/2 + 1 Gauss-Legendre points per axis):
+//   sigma mass (MGMassIntegrator, order 2p, mg_form.cpp:34-37)        p + 1
+//   convection (order OrderGrad + Order + p)                          p + 1 (1D, 2D), p + 2 (3D)
+//   time mass (MassIntegrator, order 2p + OrderW)                     p + 1 (1D, 2D), p + 2 (3D)
+//   face mass (order 2 max(p1, p2), sweep.cpp:1201-1211)              p + 1
+//   source domain (DomainLFIntegrator, order 2p)                      p + 1
+//   source boundary (BoundaryFlowIntegrator, order OrderW + 2p)       p + 1 (2D), p + 2 (3D)
+// Lumped parts use the reference-cell vertices with equal weights
+// (LumpedIntegrationRule, lumping.cpp:3-12).
+RefTables make_ref_tables(int dim, int p, int lump) {
+    RefTables t{};
+    t.dim = dim; t.p = p; t.n1 = p + 1;
+    t.n = 1; t.nf = 1;
+    for (int d = 0; d < dim; ++d) t.n *= t.n1;
+    for (int d = 0; d < dim - 1; ++d) t.nf *= t.n1;
+    t.nface = 2 * dim;
+    gauss_lobatto01(p, t.nodes);
+    const int hi = (dim == 3) ? p + 2 : p + 1;
+    set_rule(t, 0, p + 1, lump & ALLIUM_LUMP_MASS);
+    set_rule(t, 1, hi, lump & ALLIUM_LUMP_GRADIENT);
+    set_rule(t, 2, hi, lump & ALLIUM_LUMP_MASS);
+    set_rule(t, 3, p + 1, lump & ALLIUM_LUMP_FACE);
+    set_rule(t, 4, p + 1, false);
+    set_rule(t, 5, hi, false);
+    return t;
+}
+
+// ------------------------------------------------------------ face normals
+// unit normal at the face centre, out of element 1 (sweep.cpp:142-154)
+__global__ void k_face_normals(RefTables t, int nfaces, const int* __restrict__ e1k1,
+                               const double* __restrict__ corners, double* __restrict__ normals) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nfaces) return;
+    const int dim = t.dim, nc = 1 << dim;
+    const int e = e1k1[2 * f], k = e1k1[2 * f + 1];
+    double X[24];
+    for (int q = 0; q < nc * dim; ++q) X[q] = corners[(size_t)e * nc * dim + q];
+    const double tc[2] = {0.5, 0.5};
+    double xi[3], J[3][3], A[3][3];
+    face_to_cell(dim, k, tc, xi);
+    cell_jacobian(dim, X, xi, J, nullptr);
+    adjugate(dim, J, A);
+    const int ax = k / 2;
+    const double sg = (k % 2) ? 1.0 : -1.0;
+    double nr[3], nn = 0.0;
+    for (int r = 0; r < dim; ++r) { nr[r] = sg * A[ax][r]; nn += nr[r] * nr[r]; }
+    const double inv = 1.0 / sqrt(nn);
+    for (int r = 0; r < dim; ++r) normals[(size_t)f * dim + r] = nr[r] * inv;
+}
+
+cudaError_t launch_face_normals(Handle& h) {
+    const int b = 128;
+    k_face_normals<<<(h.nfaces + b - 1) / b, b, 0, h.stream>>>(h.ref, h.nfaces, h.d_face_e1k1, h.d_corners, h.d_normals);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ assembly
+// One block per cell.  Geometric factors of each quadrature point are staged
+// in shared memory, then the threads share out the matrix entries.
+//   G_d(i,j) = - sum_q w_q phi_j(q) grad_ref phi_i(q) . adj(J_q) e_d      (ConservativeConvection)
+//   M(i,j)   =   sum_q w_q det(J_q) phi_i(q) phi_j(q)                     (unit mass)
+//   F_k(i,j) =   sum_q w_q |J_face(q)| phi_i(q) phi_j(q) over face DOFs   (FaceMassMatrices)
+constexpr int kMaxPts = kMaxRule * kMaxRule * kMaxRule;
+
+struct Tab1D {
+    double v[kMaxRule][kMaxOrder + 1], d[kMaxRule][kMaxOrder + 1];
+};
+
+__device__ void tab_fill(const RefTables& t, int r, Tab1D& tb) {
+    for (int q = threadIdx.x; q < t.rn[r]; q += blockDim.x)
+        lagrange1d(t.n1, t.nodes, t.rx[r][q], tb.v[q], tb.d[q]);
+}
+
+// point index q of a tensor rule with m points per axis -> per-axis indices
+__device__ inline void split_point(int dim, int m, int q, int* id) {
+    for (int d = 0; d < dim; ++d) { id[d] = q % m; q /= m; }
+}
+
+__global__ void __launch_bounds__(128) k_assemble(RefTables t, const double* __restrict__ corners,
+                                                  double* __restrict__ Gout, double* __restrict__ Mout,
+                                                  double* __restrict__ Fout, int mass_rule, int do_conv) {
+    const int e = blockIdx.x;
+    const int dim = t.dim, n = t.n, n1 = t.n1, nc = 1 << dim, nf = t.nf, nface = t.nface;
+    __shared__ double X[24];
+    __shared__ Tab1D tm, tg, tf;
+    __shared__ double wdet[kMaxPts];
+    __shared__ double wadj[kMaxPts][3][3];
+    __shared__ double wface[6][kMaxRule * kMaxRule];
+    for (int q = threadIdx.x; q < nc * dim; q += blockDim.x) X[q] = corners[(size_t)e * nc * dim + q];
+    tab_fill(t, mass_rule, tm);
+    tab_fill(t, 1, tg);
+    tab_fill(t, 3, tf);
+    __syncthreads();
+
+    const int mm = t.rn[mass_rule], mg = t.rn[1], mf = t.rn[3];
+    int npm = 1, npg = 1, npf = 1;
+    for (int d = 0; d < dim; ++d) { npm *= mm; npg *= mg; }
+    for (int d = 0; d < dim - 1; ++d) npf *= mf;
+    for (int q = threadIdx.x; q < npm; q += blockDim.x) {
+        int id[3]; split_point(dim, mm, q, id);
+        double xi[3], J[3][3], A[3][3], w = 1.0;
+        for (int d = 0; d < dim; ++d) { xi[d] = t.rx[mass_rule][id[d]]; w *= t.rw[mass_rule][id[d]]; }
+        cell_jacobian(dim, X, xi, J, nullptr);
+        wdet[q] = adjugate(dim, J, A) * w;
+    }
+    if (do_conv) {
+        for (int q = threadIdx.x; q < npg; q += blockDim.x) {
+            int id[3]; split_point(dim, mg, q, id);
+            double xi[3], J[3][3], A[3][3], w = 1.0;
+            for (int d = 0; d < dim; ++d) { xi[d] = t.rx[1][id[d]]; w *= t.rw[1][id[d]]; }
+            cell_jacobian(dim, X, xi, J, nullptr);
+            adjugate(dim, J, A);
+            for (int d = 0; d < dim; ++d)
+                for (int r = 0; r < dim; ++r) wadj[q][d][r] = -w * A[r][d];
+        }
+        for (int q = threadIdx.x; q < nface * npf; q += blockDim.x) {
+            const int k = q / npf, qq = q % npf;
+            int id[3]; split_point(dim - 1, mf, qq, id);
+            double tt[2] = {0.0, 0.0}, w = 1.0;
+            for (int d = 0; d < dim - 1; ++d) { tt[d] = t.rx[3][id[d]]; w *= t.rw[3][id[d]]; }
+            double xi[3], J[3][3], A[3][3];
+            face_to_cell(dim, k, tt, xi);
+            cell_jacobian(dim, X, xi, J, nullptr);
+            adjugate(dim, J, A);
+            double jf = 1.0;
+            if (dim > 1) {
+                double s = 0.0;
+                for (int r = 0; r < dim; ++r) s += A[k / 2][r] * A[k / 2][r];
+                jf = sqrt(s);
+            }
+            wface[k][qq] = w * jf;
+        }
+    }
+    __syncthreads();
+
+    // unit mass
+    for (int ij = threadIdx.x; ij < n * n; ij += blockDim.x) {
+        const int i = ij / n, j = ij % n;
+        int ii[3], jj[3];
+        dof_index(dim, n1, i, ii);
+        dof_index(dim, n1, j, jj);
+        double s = 0.0;
+        for (int q = 0; q < npm; ++q) {
+            int id[3]; split_point(dim, mm, q, id);
+            double pi = 1.0, pj = 1.0;
+            for (int d = 0; d < dim; ++d) { pi *= tm.v[id[d]][ii[d]]; pj *= tm.v[id[d]][jj[d]]; }
+            s += wdet[q] * pi * pj;
+        }
+        Mout[(size_t)e * n * n + ij] = s;
+    }
+    if (!do_conv) return;
+    // convection
+    for (int t3 = threadIdx.x; t3 < dim * n * n; t3 += blockDim.x) {
+        const int d = t3 / (n * n), ij = t3 % (n * n), i = ij / n, j = ij % n;
+        int ii[3], jj[3];
+        dof_index(dim, n1, i, ii);
+        dof_index(dim, n1, j, jj);
+        double s = 0.0;
+        for (int q = 0; q < npg; ++q) {
+            int id[3]; split_point(dim, mg, q, id);
+            double pj = 1.0, bi = 0.0;
+            for (int c = 0; c < dim; ++c) pj *= tg.v[id[c]][jj[c]];
+            for (int r = 0; r < dim; ++r) {
+                double gr = 1.0;
+                for (int c = 0; c < dim; ++c) gr *= (c == r) ? tg.d[id[c]][ii[c]] : tg.v[id[c]][ii[c]];
+                bi += gr * wadj[q][d][r];
+            }
+            s += pj * bi;
+        }
+        Gout[((size_t)e * dim + d) * n * n + ij] = s;
+    }
+    // face mass blocks on face DOFs
+    for (int t3 = threadIdx.x; t3 < nface * nf * nf; t3 += blockDim.x) {
+        const int k = t3 / (nf * nf), r = t3 % (nf * nf), fi = r / nf, fj = r % nf;
+        int ti[3], tj[3];
+        dof_index(dim - 1, n1, fi, ti);
+        dof_index(dim - 1, n1, fj, tj);
+        double s = 0.0;
+        for (int q = 0; q < npf; ++q) {
+            int id[3]; split_point(dim - 1, mf, q, id);
+            double pi = 1.0, pj = 1.0;
+            for (int c = 0; c < dim - 1; ++c) { pi *= tf.v[id[c]][ti[c]]; pj *= tf.v[id[c]][tj[c]]; }
+            s += pi * pj * wface[k][q];
+        }
+        Fout[((size_t)e * nface + k) * nf * nf + r] = s;
+    }
+}
+
+cudaError_t launch_assemble(Handle& h) {
+    k_assemble<<<h.ne, 128, 0, h.stream>>>(h.ref, h.d_corners, h.d_G, h.d_M, h.d_F, 0, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_time_mass(Handle& h) {
+    k_assemble<<<h.ne, 128, 0, h.stream>>>(h.ref, h.d_corners, nullptr, h.d_Mt, nullptr, 2, 0);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ levels
+// Edge rule of sweep.cpp:157-175 on one face: element 1 -> element 2 unless
+// Omega . n_face < 0 (n_face points out of element 1).
+__device__ inline bool forward_edge(int dim, const double* om, const double* nr) {
+    return !(dot_exact(dim, om, nr) < 0.0);
+}
+
+__global__ void k_indegree(int ne, int Nw, int dim, const double* __restrict__ omega,
+                           const double* __restrict__ normals, const Slot* __restrict__ slots,
+                           int* __restrict__ indeg, int* __restrict__ level,
+                           int* __restrict__ frontier, int* __restrict__ fcount) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= (long long)ne * Nw) return;
+    const int e = (int)(v / Nw), a = (int)(v % Nw), nface = 2 * dim;
+    double om[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
+    int c = 0;
+    for (int k = 0; k < nface; ++k) {
+        const Slot s = slots[(size_t)e * nface + k];
+        if (s.nbr < 0) continue;
+        const bool fwd = forward_edge(dim, om, normals + (size_t)s.face * dim);
+        if (s.side ? fwd : !fwd) ++c;
+    }
+    indeg[v] = c;
+    if (c == 0) {
+        level[v] = 0;
+        frontier[atomicAdd(fcount, 1)] = (int)v;
+    }
+}
+
+__global__ void k_kahn(int Nw, int dim, const double* __restrict__ omega, const double* __restrict__ normals,
+                       const Slot* __restrict__ slots, int* __restrict__ indeg, int* __restrict__ level,
+                       const int* __restrict__ cur, int ncur, int* __restrict__ next, int* __restrict__ ncount,
+                       int lev) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncur) return;
+    const int u = cur[t];
+    const int e = u / Nw, a = u % Nw, nface = 2 * dim;
+    double om[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
+    for (int k = 0; k < nface; ++k) {
+        const Slot s = slots[(size_t)e * nface + k];
+        if (s.nbr < 0) continue;
+        const bool fwd = forward_edge(dim, om, normals + (size_t)s.face * dim);
+        if (!(s.side ? !fwd : fwd)) continue;   // not an out-edge of u
+        const int v = s.nbr * Nw + a;
+        if (atomicSub(&indeg[v], 1) == 1) {
+            level[v] = lev + 1;
+            next[atomicAdd(ncount, 1)] = v;
+        }
+    }
+}
+
+__global__ void k_iota(int* x, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = (int)i;
+}
+
+__global__ void k_level_hist(const int* __restrict__ level, long long n, int* __restrict__ hist) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&hist[level[i]], 1);
+}
+
+#define CK(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { h.last_error = cudaGetErrorString(_e); return ALLIUM_ERR_CUDA; } } while (0)
+
+int compute_levels(Handle& h) {
+    const long long N = (long long)h.ne * h.Nw;
+    if (N > 0x7fffffffLL) { h.last_error = "more than 2^31 (cell, angle) nodes"; return ALLIUM_ERR_SIZE; }
+    int *d_indeg = nullptr, *d_fa = nullptr, *d_fb = nullptr, *d_cnt = nullptr, *d_keys = nullptr, *d_vals = nullptr;
+    CK(cudaMalloc(&d_indeg, N * sizeof(int)));
+    CK(cudaMalloc(&d_fa, N * sizeof(int)));
+    CK(cudaMalloc(&d_fb, N * sizeof(int)));
+    CK(cudaMalloc(&d_cnt, 2 * sizeof(int)));
+    CK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(int), h.stream));
+    const int b = 256;
+    const unsigned gN = (unsigned)((N + b - 1) / b);
+    k_indegree<<<gN, b, 0, h.stream>>>(h.ne, h.Nw, h.dim, h.d_omega, h.d_normals, h.d_slots, d_indeg, h.d_level, d_fa, d_cnt);
+    CK(cudaGetLastError());
+    int ncur = 0;
+    CK(cudaMemcpyAsync(&ncur, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    CK(cudaStreamSynchronize(h.stream));
+    long long done = 0;
+    int lev = 0;
+    while (ncur > 0) {
+        done += ncur;
+        CK(cudaMemsetAsync(d_cnt + 1, 0, sizeof(int), h.stream));
+        k_kahn<<<(ncur + b - 1) / b, b, 0, h.stream>>>(h.Nw, h.dim, h.d_omega, h.d_normals, h.d_slots, d_indeg,
+                                                        h.d_level, d_fa, ncur, d_fb, d_cnt + 1, lev);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(&ncur, d_cnt + 1, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+        CK(cudaStreamSynchronize(h.stream));
+        std::swap(d_fa, d_fb);
+        ++lev;
+    }
+    cudaFree(d_fb); cudaFree(d_fa); cudaFree(d_indeg);
+    if (done != N) {
+        cudaFree(d_cnt);
+        h.last_error = "the upwind graph has a cycle";
+        return ALLIUM_ERR_NOT_DAG;
+    }
+    h.num_levels = lev;
+    // nodes sorted by level, stable in node id -> (level, cell, angle) order
+    CK(cudaMalloc(&d_keys, N * sizeof(int)));
+    CK(cudaMalloc(&d_vals, N * sizeof(int)));
+    k_iota<<<gN, b, 0, h.stream>>>(d_vals, N);
+    CK(cudaGetLastError());
+    int end_bit = 1;
+    while ((1 << end_bit) <= lev) ++end_bit;
+    size_t tmp_bytes = 0;
+    CK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, h.d_level, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
+    void* tmp = nullptr;
+    CK(cudaMalloc(&tmp, tmp_bytes));
+    CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, h.d_level, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
+    int* d_hist = nullptr;
+    CK(cudaMalloc(&d_hist, lev * sizeof(int)));
+    CK(cudaMemsetAsync(d_hist, 0, lev * sizeof(int), h.stream));
+    k_level_hist<<<gN, b, 0, h.stream>>>(h.d_level, N, d_hist);
+    CK(cudaGetLastError());
+    std::vector<int> hist(lev);
+    CK(cudaMemcpyAsync(hist.data(), d_hist, lev * sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    CK(cudaStreamSynchronize(h.stream));
+    h.h_level_offsets.assign(lev + 1, 0);
+    for (int l = 0; l < lev; ++l) h.h_level_offsets[l + 1] = h.h_level_offsets[l] + hist[l];
+    cudaFree(d_hist); cudaFree(tmp); cudaFree(d_vals); cudaFree(d_keys); cudaFree(d_cnt);
+    return ALLIUM_OK;
+}
+
+// ------------------------------------------------------------ source
+// FormTransportSource (sweep.cpp:1135-1185) for a piecewise-constant isotropic
+// density and an isotropic inflow per boundary attribute:
+//   q(g,a,i) = sum_q w_q det J Q_{g,e} phi_i
+//            + sum_{bdr faces} sum_q w_q (|Omega.n_q| - Omega.n_q)/2 psi_in phi_i
+// with n_q the unnormalised normal (CalcOrtho) at each face point
+// (BoundaryFlowIntegrator with alpha = -1, beta = -1/2).
+__global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw, int G, long long ndof,
+                                                     const double* __restrict__ corners, const double* __restrict__ omega,
+                                                     const Slot* __restrict__ slots, const double* __restrict__ qcell,
+                                                     const double* __restrict__ inflow, int nattr, double* __restrict__ out) {
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)G * Nw * ne) return;
+    const int e = (int)(tid % ne);
+    const long long r = tid / ne;
+    const int a = (int)(r % Nw), g = (int)(r / Nw);
+    const int dim = t.dim, n = t.n, n1 = t.n1, nc = 1 << dim;
+    double X[24];
+    for (int q = 0; q < nc * dim; ++q) X[q] = corners[(size_t)e * nc * dim + q];
+    double acc[64];
+    for (int i = 0; i < n; ++i) acc[i] = 0.0;
+    const double Q = qcell ? qcell[(size_t)g * ne + e] : 0.0;
+    const int m4 = t.rn[4];
+    int np = 1;
+    for (int d = 0; d < dim; ++d) np *= m4;
+    if (Q != 0.0) {
+        for (int q = 0; q < np; ++q) {
+            int id[3], rq = q;
+            double xi[3], w = 1.0;
+            for (int d = 0; d < dim; ++d) { id[d] = rq % m4; rq /= m4; xi[d] = t.rx[4][id[d]]; w *= t.rw[4][id[d]]; }
+            double J[3][3], A[3][3];
+            cell_jacobian(dim, X, xi, J, nullptr);
+            const double val = adjugate(dim, J, A) * Q;
+            double v[3][kMaxOrder + 1];
+            for (int d = 0; d < dim; ++d) lagrange1d(n1, t.nodes, xi[d], v[d], nullptr);
+            for (int i = 0; i < n; ++i) {
+                int ii[3]; dof_index(dim, n1, i, ii);
+                double ph = 1.0;
+                for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
+                acc[i] += w * val * ph;
+            }
+        }
+    }
+    if (inflow) {
+        double om[3] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
+        const int m5 = t.rn[5];
+        int npf = 1;
+        for (int d = 0; d < dim - 1; ++d) npf *= m5;
+        for (int k = 0; k < 2 * dim; ++k) {
+            const Slot s = slots[(size_t)e * 2 * dim + k];
+            if (s.nbr >= 0 || s.attr < 0 || s.attr >= nattr) continue;
+            const double fin = inflow[(size_t)g * nattr + s.attr];
+            if (fin == 0.0) continue;
+            for (int q = 0; q < npf; ++q) {
+                int id[3], rq = q;
+                double tt[2] = {0, 0}, w = 1.0;
+                for (int d = 0; d < dim - 1; ++d) { id[d] = rq % m5; rq /= m5; tt[d] = t.rx[5][id[d]]; w *= t.rw[5][id[d]]; }
+                double xi[3], J[3][3], A[3][3];
+                face_to_cell(dim, k, tt, xi);
+                cell_jacobian(dim, X, xi, J, nullptr);
+                adjugate(dim, J, A);
+                const double sg = (k % 2) ? 1.0 : -1.0;
+                double un = 0.0;
+                for (int d = 0; d < dim; ++d) un += om[d] * (sg * A[k / 2][d]);
+                const double wt = (0.5 * -1.0 * un - (-0.5) * fabs(un)) * (w * fin);
+                double v[3][kMaxOrder + 1];
+                for (int d = 0; d < dim; ++d) lagrange1d(n1, t.nodes, xi[d], v[d], nullptr);
+                for (int i = 0; i < n; ++i) {
+                    int ii[3]; dof_index(dim, n1, i, ii);
+                    double ph = 1.0;
+                    for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
+                    acc[i] += wt * ph;
+                }
+            }
+        }
+    }
+    double* o = out + psi_index(ndof, Nw, g, a, (long long)e * n);
+    for (int i = 0; i < n; ++i) o[i] = acc[i];
+}
+
+cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out) {
+    const long long total = (long long)h.G * h.Nw * h.ne;
+    const int b = 128;
+    k_form_source<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.ref, h.ne, h.Nw, h.G, h.ndof, h.d_corners, h.d_omega,
+                                                                       h.d_slots, q_cell, inflow, nattr, out);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ moments
+// DiscreteToMoment::Mult (transport_op.cpp:3-31).  The sums run over angles in
+// order with separate multiply and add roundings, as the reference loop does.
+__global__ void k_moments(int Nw, int G, int dim, long long ndof, const double* __restrict__ omega,
+                          const double* __restrict__ w, const double* __restrict__ psi, double* __restrict__ phi, int nmom) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    double acc = 0.0;
+    for (int a = 0; a < Nw; ++a) acc = __dadd_rn(acc, __dmul_rn(w[a], psi[psi_index(ndof, Nw, g, a, s)]));
+    phi[s + ndof * g] = acc;
+    for (int m = 0; m + 1 < nmom; ++m) {
+        double am = 0.0;
+        for (int a = 0; a < Nw; ++a)
+            am = __dadd_rn(am, __dmul_rn(__dmul_rn(omega[a * dim + m], w[a]), psi[psi_index(ndof, Nw, g, a, s)]));
+        phi[s + ndof * (g + (long long)G * (1 + m))] = am;
+    }
+}
+
+// MultTranspose / AddMultTranspose (transport_op.cpp:33-89)
+__global__ void k_moments_transpose(int Nw, int G, int dim, long long ndof, const double* __restrict__ omega,
+                                    double wsum, const double* __restrict__ phi, double* __restrict__ psi,
+                                    int nmom, double alpha, int add) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * Nw * ndof) return;
+    const long long s = t % ndof;
+    const long long r = t / ndof;
+    const int a = (int)(r % Nw), g = (int)(r / Nw);
+    double* p = psi + psi_index(ndof, Nw, g, a, s);
+    const double p0 = phi[s + ndof * g];
+    double v = add ? __dadd_rn(*p, __ddiv_rn(__dmul_rn(alpha, p0), wsum)) : __ddiv_rn(p0, wsum);
+    for (int m = 0; m + 1 < nmom; ++m) {
+        const double ph = phi[s + ndof * (g + (long long)G * (1 + m))];
+        const double om = omega[a * dim + m];
+        const double c = add ? __dmul_rn(__dmul_rn(__dmul_rn(alpha, 3.0), om), ph) : __dmul_rn(__dmul_rn(3.0, om), ph);
+        v = __dadd_rn(v, __ddiv_rn(c, wsum));
+    }
+    *p = v;
+}
+
+cudaError_t launch_moments(Handle& h, const double* psi, double* phi, int nmom) {
+    const long long total = (long long)h.G * h.ndof;
+    const int b = 256;
+    k_moments<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.Nw, h.G, h.dim, h.ndof, h.d_omega, h.d_weights, psi, phi, nmom);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_moments_transpose(Handle& h, const double* phi, double* psi, int nmom, double alpha, int add) {
+    const long long total = (long long)h.G * h.Nw * h.ndof;
+    const int b = 256;
+    k_moments_transpose<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.Nw, h.G, h.dim, h.ndof, h.d_omega, h.wsum,
+                                                                            phi, psi, nmom, alpha, add);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ balance
+// ComputeBalance (sweep.cpp:1400-1462): sum over (g, a, e) of
+//   w_a * 1^T (sigma M + tau Mt) psi_e   +   leakage of outflow boundary faces
+//   w_a * (Omega.n) * 1^T F_self psi_e|face.
+// Each block writes one partial sum; a second pass adds them in order, so the
+// result does not depend on scheduling.
+constexpr int kBalanceBlock = 256;
+
+__global__ void __launch_bounds__(kBalanceBlock) k_balance(RefTables t, int ne, int Nw, int G, long long ndof,
+                                                           const double* __restrict__ omega, const double* __restrict__ w,
+                                                           const double* __restrict__ normals, const Slot* __restrict__ slots,
+                                                           const double* __restrict__ M, const double* __restrict__ Mt,
+                                                           const double* __restrict__ F, const double* __restrict__ sigma,
+                                                           double tau, int td, const double* __restrict__ psi,
+                                                           double* __restrict__ partial) {
+    const int dim = t.dim, n = t.n, nf = t.nf, nface = t.nface;
+    const long long total = (long long)G * ne * Nw;
+    double local = 0.0;
+    for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total;
+         tid += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(tid % Nw);
+        const long long r = tid / Nw;
+        const int e = (int)(r % ne), g = (int)(r / ne);
+        const double* x = psi + psi_index(ndof, Nw, g, a, (long long)e * n);
+        const double* Me = M + (size_t)e * n * n;
+        const double sg = sigma[(size_t)g * ne + e];
+        double absb = 0.0;
+        for (int i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int j = 0; j < n; ++j) {
+                double m = sg * Me[i * n + j];
+                if (td) m += tau * Mt[(size_t)e * n * n + i * n + j];
+                s += m * x[j];
+            }
+            absb += s;
+        }
+        double contrib = absb * w[a];
+        double om[3] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
+        for (int k = 0; k < nface; ++k) {
+            const Slot s = slots[(size_t)e * nface + k];
+            if (s.nbr >= 0) continue;
+            const double dot = dot_exact(dim, om, normals + (size_t)s.face * dim);
+            if (dot < 0.0) continue;
+            const double* Fk = F + ((size_t)e * nface + k) * nf * nf;
+            double sum = 0.0;
+            for (int ii = 0; ii < nf; ++ii) {
+                double acc = 0.0;
+                for (int jj = 0; jj < nf; ++jj) acc += Fk[ii * nf + jj] * x[face_dof(dim, t.p, k, jj)];
+                sum += acc;
+            }
+            contrib += w[a] * dot * sum;
+        }
+        local += contrib;
+    }
+    __shared__ double red[kBalanceBlock];
+    red[threadIdx.x] = local;
+    __syncthreads();
+    for (int s = kBalanceBlock / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int nparts, double* __restrict__ out) {
+    __shared__ double red[kBalanceBlock];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += partial[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = kBalanceBlock / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+cudaError_t launch_balance(Handle& h, const double* psi, double* partial, int nblocks_max, int* nblocks) {
+    const long long total = (long long)h.G * h.ne * h.Nw;
+    long long want = (total + kBalanceBlock - 1) / kBalanceBlock;
+    const int nb = (int)(want < nblocks_max ? want : nblocks_max);
+    *nblocks = nb < 1 ? 1 : nb;
+    k_balance<<<*nblocks, kBalanceBlock, 0, h.stream>>>(h.ref, h.ne, h.Nw, h.G, h.ndof, h.d_omega, h.d_weights, h.d_normals,
+                                                         h.d_slots, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.tau,
+                                                         h.time_dependent ? 1 : 0, psi, partial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_balance_finish(Handle& h, const double* partial, int nparts, double* out) {
+    k_sum_partials<<<1, kBalanceBlock, 0, h.stream>>>(partial, nparts, out);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ scattering source
+// q(g,a,e.) = q_fixed(g,a,e.) + (sigma_s[g][e] Ms_e phi(g,e.)) / sum_w
+// with Ms_e the MassIntegrator matrix (rule order 2p + OrderW; vertex rule when
+// the mass is lumped): the S.Mult -> D.MultTranspose -> psi += source chain of
+// MomentMethodFixedPointOperator::Mult (transport_op.hpp:75-90).
+__global__ void k_scatter_source(int ne, int Nw, int G, int n, long long ndof, double wsum,
+                                 const double* __restrict__ Ms, const double* __restrict__ sigma_s,
+                                 const double* __restrict__ phi, const double* qfix, double* out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    const int e = (int)(s / n), i = (int)(s % n);
+    const double* M = Ms + (size_t)e * n * n + (size_t)i * n;
+    const double* ph = phi + ndof * g + (long long)e * n;
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) acc += M[j] * ph[j];
+    const double v = (sigma_s[(size_t)g * ne + e] * acc) / wsum;
+    for (int a = 0; a < Nw; ++a) {
+        const long long k = psi_index(ndof, Nw, g, a, s);
+        out[k] = qfix ? qfix[k] + v : v;
+    }
+}
+
+cudaError_t launch_scatter_source(Handle& h, const double* sigma_s, const double* phi, const double* qfix, double* out) {
+    const long long total = (long long)h.G * h.ndof;
+    const int b = 256;
+    k_scatter_source<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.ne, h.Nw, h.G, h.n, h.ndof, h.wsum, h.d_Mt,
+                                                                          sigma_s, phi, qfix, out);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ FP32 copies
+__global__ void k_to_f32(const double* __restrict__ in, float* __restrict__ out, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
+static cudaError_t to_f32(Handle& h, const double* in, float** out, long long n) {
+    if (!in || n == 0) return cudaSuccess;
+    if (!*out) {
+        cudaError_t e = cudaMalloc(out, n * sizeof(float));
+        if (e != cudaSuccess) return e;
+    }
+    k_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, h.stream>>>(in, *out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t make_fp32_copies(Handle& h) {
+    const long long nn = (long long)h.n * h.n;
+    cudaError_t e;
+    if ((e = to_f32(h, h.d_G, &h.f_G, (long long)h.ne * h.dim * nn)) != cudaSuccess) return e;
+    if ((e = to_f32(h, h.d_M, &h.f_M, (long long)h.ne * nn)) != cudaSuccess) return e;
+    if ((e = to_f32(h, h.d_F, &h.f_F, (long long)h.ne * h.nface * h.nf * h.nf)) != cudaSuccess) return e;
+    if ((e = to_f32(h, h.d_sigma, &h.f_sigma, (long long)h.G * h.ne)) != cudaSuccess) return e;
+    if (h.time_dependent && (e = to_f32(h, h.d_Mt, &h.f_Mt, (long long)h.ne * nn)) != cudaSuccess) return e;
+    h.fp32_ready = true;
+    return cudaSuccess;
+}
+
+}  // namespace allium

@@ -1,0 +1,47 @@
+// FP64 sweep (partially pivoted local LU) and the FP64 forward operator.
+#include "sweep_launch.cuh"
+
+namespace allium {
+
+cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
+    SweepArgs<double> a;
+    a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
+    a.omega = h.d_omega; a.normals = h.d_normals; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
+    a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
+    a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
+    a.src = src; a.psi = psi; a.status = h.d_status;
+    return sweep_dispatch<double, true>(h, a);
+}
+
+template <int D, int P>
+cudaError_t apply_L_launch(Handle& h, const ApplyArgs& a) {
+    constexpr int kBlock = 128;
+    const long long total = (long long)h.G * h.ne * h.Nw;
+    const unsigned grid = (unsigned)((total + kBlock - 1) / kBlock);
+    k_apply_L<D, P><<<grid, kBlock, 0, h.stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y) {
+    ApplyArgs a;
+    a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
+    a.omega = h.d_omega; a.normals = h.d_normals; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
+    a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
+    a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
+    a.x = x; a.y = y;
+    switch (h.dim * 10 + h.p) {
+        case 10: return apply_L_launch<1, 0>(h, a);
+        case 11: return apply_L_launch<1, 1>(h, a);
+        case 12: return apply_L_launch<1, 2>(h, a);
+        case 13: return apply_L_launch<1, 3>(h, a);
+        case 20: return apply_L_launch<2, 0>(h, a);
+        case 21: return apply_L_launch<2, 1>(h, a);
+        case 22: return apply_L_launch<2, 2>(h, a);
+        case 23: return apply_L_launch<2, 3>(h, a);
+        case 30: return apply_L_launch<3, 0>(h, a);
+        case 31: return apply_L_launch<3, 1>(h, a);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+}  // namespace allium

@@ -1,0 +1,268 @@
+"""Python mirror of allium's sweep-path operators, backed by liballium_sweep.so.
+
+Names, argument meaning and in-place behaviour follow the reference:
+  InverseAdvectionOperator   src/sweep.hpp:13-130   (Mult, AssembleLocalMatrices,
+                                                     SetTimeAbsorption, UseParallelBlockJacobi)
+  AdvectionOperator          src/sweep.hpp:155-166  (Mult, ComputeBalance)
+  DiscreteToMoment           src/transport_op.hpp:97-122
+  TransportOperator          src/transport_op.hpp:9-35
+  FormTransportSource        src/sweep.cpp:1135-1185 (isotropic, piecewise constant data)
+
+Vectors may be numpy arrays (host) or torch tensors (CUDA or pinned host),
+float64 in allium's RIGHT layout psi[g, a, i] -> i + Ndof (a + Nw g).  Calls on
+host arrays return when the result is on the host; calls on CUDA tensors are
+ordered on the torch stream that was current when the operator was built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import BcDesc, FeDesc, MeshDesc, QuadDesc, check
+
+try:  # torch is plumbing only: device memory and streams
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _ptr(x, dtype, size=None, what="array"):
+    """Raw pointer of a numpy array or torch tensor after dtype/size checks."""
+    if torch is not None and isinstance(x, torch.Tensor):
+        want = torch.float64 if dtype == np.float64 else (torch.float32 if dtype == np.float32 else torch.int32)
+        if x.dtype != want or not x.is_contiguous():
+            raise TypeError(f"{what} must be a contiguous {want} tensor")
+        if size is not None and x.numel() != size:
+            raise ValueError(f"{what} has {x.numel()} entries, expected {size}")
+        return x.data_ptr()
+    if not isinstance(x, np.ndarray) or x.dtype != dtype or not x.flags.c_contiguous:
+        raise TypeError(f"{what} must be a contiguous {np.dtype(dtype).name} numpy array")
+    if size is not None and x.size != size:
+        raise ValueError(f"{what} has {x.size} entries, expected {size}")
+    return x.ctypes.data
+
+
+class InverseAdvectionOperator:
+    """L^{-1}: the upwind DG sweep on one GPU.
+
+    mesh: allium_gb300.mesh.Mesh; order: DG order (0..3, Gauss-Lobatto basis);
+    quad: allium_gb300.quadrature.AngularQuadrature; sigma_t: [G, Ne] total cross
+    section per cell; lump: allium lumping bit mask; bc: {attribute: "inflow"}.
+    """
+
+    def __init__(self, mesh, order, quad, sigma_t, lump=0, bc=None):
+        L = _lib.lib()
+        self.mesh, self.order, self.quad, self.lump = mesh, int(order), quad, int(lump)
+        self.dim = mesh.dim
+        sig = np.ascontiguousarray(sigma_t, dtype=np.float64).reshape(-1, mesh.num_elements)
+        self.G = sig.shape[0]
+        self.Nw = quad.size
+        self.n = (self.order + 1) ** self.dim
+        self.ndof = mesh.num_elements * self.n
+        self._keep = [np.ascontiguousarray(mesh.vertices, dtype=np.float64),
+                      np.ascontiguousarray(mesh.elements, dtype=np.int32),
+                      np.ascontiguousarray(mesh.boundary_faces, dtype=np.int32),
+                      np.ascontiguousarray(mesh.boundary_attributes, dtype=np.int32),
+                      np.ascontiguousarray(quad.omega, dtype=np.float64),
+                      np.ascontiguousarray(quad.weights, dtype=np.float64), sig]
+        v, e, bf, ba, om, w, s = self._keep
+        md = MeshDesc(self.dim, v.shape[0], v.ctypes.data, e.shape[0], e.ctypes.data,
+                      ba.shape[0], bf.ctypes.data, ba.ctypes.data)
+        fd = FeDesc(self.order, 0, self.lump)
+        qd = QuadDesc(self.dim, self.Nw, om.ctypes.data, w.ctypes.data)
+        bcd = None
+        if bc:
+            kinds = {"inflow": 0, "reflective": 1}
+            attrs = np.array(list(bc.keys()), dtype=np.int32)
+            kd = np.array([kinds[str(k).lower()] for k in bc.values()], dtype=np.int32)
+            self._keep += [attrs, kd]
+            bcd = C.pointer(BcDesc(len(attrs), attrs.ctypes.data, kd.ctypes.data))
+        h = C.c_void_p()
+        st = L.allium_sweep_create(C.byref(md), C.byref(fd), C.byref(qd), self.G, s.ctypes.data, bcd, C.byref(h))
+        check(st)
+        self.h = h
+        self.pbj = False
+        self.num_pbj_sweeps = 1
+        if torch is not None and torch.cuda.is_available():
+            self.set_stream(torch.cuda.current_stream())
+        psi_size, ndof, nlev = C.c_longlong(), C.c_longlong(), C.c_int()
+        check(L.allium_sweep_sizes(self.h, C.byref(psi_size), C.byref(ndof), C.byref(nlev)), self.h)
+        self.height = self.width = int(psi_size.value)
+        self.num_levels = int(nlev.value)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            _lib.lib().allium_sweep_destroy(h)
+            self.h = None
+
+    # --- reference surface
+    def Height(self):
+        return self.height
+
+    def Width(self):
+        return self.width
+
+    def set_stream(self, stream):
+        ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else (stream or 0)
+        check(_lib.lib().allium_sweep_set_stream(self.h, C.c_void_p(ptr)), self.h)
+
+    def Mult(self, source, psi):
+        """psi = L^{-1} source (FP64); source may be psi itself."""
+        sp = _ptr(source, np.float64, self.width, "source")
+        pp = _ptr(psi, np.float64, self.height, "psi")
+        sweeps = self.num_pbj_sweeps if self.pbj else 1
+        if sweeps > 1 and sp == pp:
+            # the reference keeps a copy of the source when it sweeps more than once
+            source = source.copy() if isinstance(source, np.ndarray) else source.clone()
+            sp = _ptr(source, np.float64, self.width, "source")
+        for _ in range(sweeps):
+            # on one GPU the block Jacobi sweep has no off-rank data to lag and
+            # is the upwind sweep itself
+            check(_lib.lib().allium_sweep_mult(self.h, C.c_void_p(sp), C.c_void_p(pp)), self.h)
+
+    def MultF32(self, source, psi):
+        """FP32 sweep (storage and local solves in FP32)."""
+        check(_lib.lib().allium_sweep_mult_f32(self.h, C.c_void_p(_ptr(source, np.float32, self.width, "source")),
+                                               C.c_void_p(_ptr(psi, np.float32, self.height, "psi"))), self.h)
+
+    def AssembleLocalMatrices(self, sigma_t=None):
+        if sigma_t is None:
+            sigma_t = self._keep[6]
+        sig = np.ascontiguousarray(sigma_t, dtype=np.float64).reshape(self.G, -1)
+        self._keep[6] = sig
+        check(_lib.lib().allium_sweep_assemble(self.h, C.c_void_p(sig.ctypes.data)), self.h)
+
+    def SetTimeAbsorption(self, tau):
+        self.time_absorption = float(tau)
+        check(_lib.lib().allium_sweep_set_time_absorption(self.h, float(tau)), self.h)
+
+    def GetTimeAbsorption(self):
+        return getattr(self, "time_absorption", 0.0)
+
+    def UseParallelBlockJacobi(self, use=True):
+        self.pbj = bool(use)
+
+    def IsParallelBlockJacobi(self):
+        return self.pbj
+
+    def SetNumPBJSweeps(self, n):
+        self.num_pbj_sweeps = int(n)
+
+    def Exchange(self, psi):
+        """PBJ ghost exchange; a single GPU owns every cell, so nothing moves."""
+        return None
+
+    def GetLumpingType(self):
+        return self.lump
+
+    def levels(self):
+        lev = np.empty(self.mesh.num_elements * self.Nw, dtype=np.int32)
+        check(_lib.lib().allium_sweep_levels(self.h, C.c_void_p(lev.ctypes.data)), self.h)
+        return lev
+
+    def synchronize(self):
+        check(_lib.lib().allium_sweep_synchronize(self.h), self.h)
+
+
+class AdvectionOperator:
+    """Forward operator L sharing the sweep's matrices (src/sweep.hpp:155-166)."""
+
+    def __init__(self, Linv: InverseAdvectionOperator):
+        self.Linv = Linv
+        self.height = self.width = Linv.height
+
+    def Mult(self, x, y):
+        L = self.Linv
+        check(_lib.lib().allium_sweep_apply_L(L.h, C.c_void_p(_ptr(x, np.float64, L.width, "x")),
+                                              C.c_void_p(_ptr(y, np.float64, L.height, "y"))), L.h)
+
+    def ComputeBalance(self, psi):
+        L = self.Linv
+        out = np.zeros(1)
+        check(_lib.lib().allium_sweep_balance(L.h, C.c_void_p(_ptr(psi, np.float64, L.width, "psi")),
+                                              C.c_void_p(out.ctypes.data)), L.h)
+        return float(out[0])
+
+
+class DiscreteToMoment:
+    """phi = D psi and its transposes (src/transport_op.cpp:3-89)."""
+
+    def __init__(self, Linv: InverseAdvectionOperator, num_moments=1):
+        if num_moments not in (1, Linv.dim + 1):
+            raise ValueError("num_moments must be 1 or dim + 1")
+        self.Linv = Linv
+        self.num_moments = num_moments
+        self.height = Linv.G * num_moments * Linv.ndof
+        self.width = Linv.width
+
+    def Mult(self, psi, phi):
+        L = self.Linv
+        check(_lib.lib().allium_sweep_moments(L.h, C.c_void_p(_ptr(psi, np.float64, self.width, "psi")),
+                                              C.c_void_p(_ptr(phi, np.float64, self.height, "phi")),
+                                              self.num_moments), L.h)
+
+    def MultTranspose(self, phi, psi):
+        self._transpose(phi, psi, 1.0, 0)
+
+    def AddMultTranspose(self, phi, psi, alpha=1.0):
+        self._transpose(phi, psi, alpha, 1)
+
+    def _transpose(self, phi, psi, alpha, add):
+        L = self.Linv
+        check(_lib.lib().allium_sweep_moments_transpose(
+            L.h, C.c_void_p(_ptr(phi, np.float64, self.height, "phi")),
+            C.c_void_p(_ptr(psi, np.float64, self.width, "psi")), self.num_moments, float(alpha), int(add)), L.h)
+
+
+def ScatteringSource(Linv: InverseAdvectionOperator, sigma_s, phi, q_fixed=None, out=None):
+    """out = D^T (S phi) + q_fixed with S = sigma_s[G, Ne] x MassIntegrator matrix
+    (the source-iteration update of transport_op.hpp:75-90)."""
+    if out is None:
+        out = np.empty(Linv.width)
+    sig = np.ascontiguousarray(sigma_s, dtype=np.float64).reshape(Linv.G, -1)
+    qp = _ptr(q_fixed, np.float64, Linv.width, "q_fixed") if q_fixed is not None else None
+    check(_lib.lib().allium_sweep_scattering_source(
+        Linv.h, C.c_void_p(sig.ctypes.data), C.c_void_p(_ptr(phi, np.float64, Linv.G * Linv.ndof, "phi")),
+        C.c_void_p(qp), C.c_void_p(_ptr(out, np.float64, Linv.width, "out"))), Linv.h)
+    return out
+
+
+def FormTransportSource(Linv: InverseAdvectionOperator, q_cell=None, inflow=None, out=None):
+    """Weak-form source for an isotropic density q_cell[G, Ne] and an isotropic
+    inflow[G, num_attr] indexed by boundary attribute (vacuum where 0)."""
+    L = _lib.lib()
+    if out is None:
+        out = np.empty(Linv.width)
+    qp = inp = None
+    nattr = 0
+    keep = []
+    if q_cell is not None:
+        q = np.ascontiguousarray(q_cell, dtype=np.float64).reshape(Linv.G, -1)
+        keep.append(q)
+        qp = q.ctypes.data
+    if inflow is not None:
+        fin = np.ascontiguousarray(inflow, dtype=np.float64).reshape(Linv.G, -1)
+        keep.append(fin)
+        inp, nattr = fin.ctypes.data, fin.shape[1]
+    check(L.allium_sweep_form_source(Linv.h, C.c_void_p(qp), C.c_void_p(inp), nattr,
+                                     C.c_void_p(_ptr(out, np.float64, Linv.width, "source"))), Linv.h)
+    return out
+
+
+class TransportOperator:
+    """I - D L^{-1} S D^T applied to phi (src/transport_op.hpp:9-35).  S is a
+    callable phi -> S phi (the scattering mass), psi the work vector."""
+
+    def __init__(self, D: DiscreteToMoment, Linv: InverseAdvectionOperator, S, psi):
+        self.D, self.Linv, self.S, self.psi = D, Linv, S, psi
+
+    def Mult(self, x, y):
+        self.S(x, y)
+        self.D.MultTranspose(y, self.psi)
+        self.Linv.Mult(self.psi, self.psi)
+        self.D.Mult(self.psi, y)
+        y -= x
+        y *= -1.0

@@ -1,0 +1,311 @@
+"""Benchmark of the upwind DG transport sweep on the 3D chive workload.
+
+Workload: 64^3 hexes of [0,1]^3 with interior vertices jittered by U[-0.1h, 0.1h]
+(seeded; at +-0.2h every seed tried gives a cyclic S12 upwind graph, which
+allium rejects), trilinear DG (p = 1, 8 DOF/cell), level-symmetric S12 (168
+directions), one group, sigma_t log-uniform in [0.1, 100] per cell, vacuum
+boundaries, q uniform in [0, 1] per cell.  A step is one InverseAdvectionOperator
+Mult (one full sweep of every cell, angle and group).  The metric is swept
+cell-angle-group DOF per second = G * Nw * Ndof / sweep time.
+
+  value     FP64 sweep with q and psi resident in HBM (CUDA events)
+  e2e       the same Mult through the C ABI with pinned host buffers, the
+            host->device copy of q and the device->host copy of psi inside the
+            timed region (wall clock around the synchronous call)
+  fp32      the FP32 sweep (FP32 storage and local solves), resident in HBM
+
+`--impl reference` times the CPU restatement of the reference sweep (OpenMP,
+all host cores) on a sample of the same workload (8 of the 168 directions,
+one per octant, on the full mesh).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20261203
+JITTER = 0.1   # +-0.2h makes every tried seed's S12 graph cyclic; see the design doc
+CELLS = (64, 64, 64)
+ORDER = 1
+SN = 12
+METRIC = "swept cell-angle-group DOF/s"
+UNIT = "DOF*angle*group/s"
+
+
+def workload():
+    from allium_gb300 import mesh as M
+    from allium_gb300 import quadrature as Q
+    mesh = M.cartesian(CELLS, jitter=JITTER, seed=SEED)
+    quad = Q.level_symmetric(SN, 3)
+    rng = np.random.default_rng(SEED + 1)
+    sigma = 10.0 ** rng.uniform(-1.0, 2.0, size=(1, mesh.num_elements))
+    q = rng.uniform(0.0, 1.0, size=(1, mesh.num_elements))
+    return mesh, quad, sigma, q
+
+
+def config(levels=None):
+    c = {"workload": "chive 3D sweep: 64^3 hex mesh of [0,1]^3, interior vertices jittered +-0.1h (seed 20261203; +-0.2h gives a cyclic S12 upwind graph), "
+                     "p=1 Gauss-Lobatto DG (8 DOF/cell), level-symmetric S12 (168 directions), 1 group, "
+                     "sigma_t log-uniform [0.1,100] per cell, vacuum boundaries, q ~ U[0,1] per cell",
+         "cells": 64 ** 3, "dofs_per_cell": 8, "angles": 168, "groups": 1,
+         "psi_entries": 64 ** 3 * 8 * 168,
+         "l2_policy": "inputs larger than L2 (q and psi are 2.8 GB each in FP64)"}
+    if levels is not None:
+        c["levels"] = levels
+    return c
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_entry():
+    """DRAM bytes per swept entry of the FP64 sweep kernel from the committed
+    ncu summary (profiles/sweep_fp64_traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "sweep_fp64_traffic.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["dram_bytes_per_entry"])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sweep_sample(threads, steps, warmup):
+    """CPU restatement of Mult_Upwind (OpenMP) on the workload mesh with 8 of
+    the 168 directions (one per octant).  Returns DOF*angle*group/s per step."""
+    from oracle.oracle import OracleSweep
+    from allium_gb300 import quadrature as Q
+    mesh, quad, sigma, q = workload()
+    pick = [i * (quad.size // 8) for i in range(8)]
+    sub = Q.AngularQuadrature(3, quad.omega[pick].copy(), quad.weights[pick].copy())
+    o = OracleSweep(mesh, ORDER, sub, sigma)
+    src = o.form_source(q_cell=q)
+    psi = np.empty_like(src)
+    for _ in range(warmup):
+        o.mult(src, psi, threads=threads)
+    rates = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.mult(src, psi, threads=threads)
+        rates.append(o.psi_size / (time.perf_counter() - t0))
+    return rates, o.psi_size
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rates, size = cpu_sweep_sample(threads, args.steps, max(1, args.warmup))
+    v = statistics.median(rates)
+    sample = f"full 64^3 mesh, 8 of 168 S12 directions (one per octant): {size} DOF*angle per sweep"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": size / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    from allium_gb300.sweep import FormTransportSource, InverseAdvectionOperator
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    mesh, quad, sigma, q = workload()
+    L = InverseAdvectionOperator(mesh, ORDER, quad, sigma)
+    stream = torch.cuda.current_stream()
+    N = L.width
+    src_host = FormTransportSource(L, q)
+    src = torch.from_numpy(src_host).cuda()
+    psi = torch.empty_like(src)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    # --- FP64, resident in HBM
+    for _ in range(args.warmup):
+        L.Mult(src, psi)
+    L.synchronize()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            L.Mult(src, psi)
+        ev1.record(stream)
+        L.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * N / (ms * 1e-3)
+
+    # --- FP32 sweep, resident
+    f_src = src.float()
+    f_psi = torch.empty_like(f_src)
+    for _ in range(args.warmup):
+        L.MultF32(f_src, f_psi)
+    L.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        L.MultF32(f_src, f_psi)
+    ev1.record(stream)
+    L.synchronize()
+    ms32 = ev0.elapsed_time(ev1) / args.steps
+    err32 = float((torch.max(torch.abs(f_psi.double() - psi)) / torch.max(torch.abs(psi))).item())
+    del f_src, f_psi
+
+    # --- e2e through the C ABI with pinned host buffers
+    h_src = torch.from_numpy(src_host).pin_memory()
+    h_psi = torch.empty_like(h_src).pin_memory()
+    L.Mult(h_src, h_psi)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.Mult(h_src, h_psi)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * N / e2e_s
+    assert torch.equal(h_psi, psi.cpu()), "host and device paths disagree"
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel (the FP64 sweep kernel, all level launches of one Mult)
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 16.0 * N + 8.0 * mesh.num_elements * (1 + 3 * 8)
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    tpe = traffic_per_entry()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (tpe * N if tpe is not None else None), "peak_kind": peak_kind,
+            "kernel": "k_sweep_level<3,1,double,pivot>", "algorithmic_bytes_per_launch": alg_bytes,
+            "launch": "one Mult = all wavefront-level launches of the sweep kernel"}
+    # FP64 compute roofline for context: ~147 FP64 FMA per swept entry
+    fp64_flops = 2 * 590.0 * N / 8
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(L.num_levels),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
+                    "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": args.steps * L.num_levels,
+            "roofline": roof,
+            "fp64_compute": {"achieved_tflops": fp64_flops / (ms * 1e-3) / 1e12, "nominal_peak_tflops": 1.25},
+            "fp32": {"value": N / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32,
+                     "max_rel_err_vs_fp64": err32,
+                     "roofline_frac": (8.0 * N / (ms32 * 1e-3) / 1e9) / peak},
+            "clocks": clk.summary()}
+    if not args.no_cpu:
+        rates, size = cpu_sweep_sample(os.cpu_count() or 1, 3, 1)
+        line["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": f"full 64^3 mesh, 8 of 168 S12 directions (one per octant), {size} DOF*angle per sweep, median of 3"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/* allium_sweep.h -- C ABI of the GB300 upwind DG transport sweep.
+ *
+ * One handle replaces one allium InverseAdvectionOperator (src/sweep.hpp:13-130)
+ * together with the AdvectionOperator, DiscreteToMoment and FormTransportSource
+ * pieces that sit on either side of it.  All sizes are plain ints, all arrays
+ * plain pointers; there are no CUDA or torch types in the signatures (the
+ * stream is passed as void*).
+ *
+ * Vectors use allium's RIGHT transport layout (src/tvector.hpp:47-58):
+ *   psi(g, a, i) = psi[i + Ndof * (a + Nw * g)],  i = e * n + local DOF,
+ * where the local DOF order of an element is lexicographic (x fastest) over
+ * Gauss-Lobatto nodes, exactly as MFEM's L2_FECollection numbers it.
+ * Moments use MomentVectorLayout (src/tvector.hpp:68):
+ *   phi(g, m, i) = phi[i + Ndof * (g + G * m)].
+ *
+ * Every array argument may be a host pointer or a device pointer; the library
+ * asks the CUDA runtime which one it is.  Calls with host pointers stage the
+ * data through device buffers and return when the host result is written.
+ * Calls with device pointers are enqueued on the handle's stream and return
+ * at once; allium_sweep_synchronize() waits and reports any error raised by a
+ * kernel (singular local system, non-finite values).
+ *
+ * Every function returns an allium status (ALLIUM_OK = 0) and never aborts.
+ * allium_sweep_last_error() gives a one-line reason for the last failure.
+ * A handle is not thread safe: one host thread and one stream per handle.
+ */
+#ifndef ALLIUM_SWEEP_H
+#define ALLIUM_SWEEP_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct allium_sweep allium_sweep;
+
+enum allium_status {
+    ALLIUM_OK = 0,
+    ALLIUM_ERR_ARG = 1,          /* bad argument (null pointer, out of range) */
+    ALLIUM_ERR_NOT_DAG = 2,      /* upwind graph has a cycle (sweep.cpp:205-208 aborts) */
+    ALLIUM_ERR_SIZE = 3,         /* size mismatch or a size above a stated maximum */
+    ALLIUM_ERR_TIMEOUT = 4,      /* a bounded device wait gave up */
+    ALLIUM_ERR_NAN = 5,          /* non-finite value detected */
+    ALLIUM_ERR_CUDA = 6,         /* CUDA runtime error (message in last_error) */
+    ALLIUM_ERR_UNSUPPORTED = 7,  /* option not implemented (reflective, fixup, ...) */
+    ALLIUM_ERR_MESH = 8,         /* non-conforming or malformed mesh */
+    ALLIUM_ERR_SINGULAR = 9      /* zero pivot in a local solve (mfem::LinearSolve fails) */
+};
+
+enum allium_bc_kind { ALLIUM_BC_INFLOW = 0, ALLIUM_BC_REFLECTIVE = 1 };  /* src/bdr_conditions.hpp:5-10 */
+enum allium_lump { ALLIUM_LUMP_MASS = 1, ALLIUM_LUMP_GRADIENT = 2, ALLIUM_LUMP_FACE = 4 };  /* src/lumping.hpp:10-18 */
+enum allium_basis { ALLIUM_BASIS_GAUSS_LOBATTO = 0 };
+
+/* Mesh of segments (dim 1), quadrilaterals (dim 2) or hexahedra (dim 3) with
+ * (multi)linear geometry.  element_vertices uses MFEM's local vertex order:
+ * quad (0,0),(1,0),(1,1),(0,1); hex: bottom quad then top quad.  Boundary faces
+ * carry the attributes used by the boundary-condition map and the inflow
+ * source; a boundary face not listed gets attribute 0.
+ * Replaces the mfem::ParMesh / ParFiniteElementSpace pair the reference
+ * constructor takes (src/sweep.hpp:82). */
+typedef struct {
+    int dim;
+    int num_vertices;
+    const double* vertices;             /* [num_vertices][dim] */
+    int num_elements;
+    const int* element_vertices;        /* [num_elements][2^dim] */
+    int num_boundary_faces;
+    const int* boundary_face_vertices;  /* [num_boundary_faces][2^(dim-1)] */
+    const int* boundary_attributes;     /* [num_boundary_faces] */
+} allium_mesh_desc;
+
+/* L2 DG space: order p in 0..3, Gauss-Lobatto basis, lumping bit mask
+ * (allium's `lump` constructor argument, src/sweep.hpp:83). */
+typedef struct {
+    int order;
+    int basis;
+    int lump;
+} allium_fe_desc;
+
+/* Angular quadrature: directions [num_angles][dim] and weights
+ * (AngularQuadrature, src/angular_quadrature.hpp:4-22). */
+typedef struct {
+    int dim;
+    int num_angles;
+    const double* omega;
+    const double* weights;
+} allium_quad_desc;
+
+/* BoundaryConditionMap (src/bdr_conditions.hpp): attribute -> kind. */
+typedef struct {
+    int num;
+    const int* attributes;
+    const int* kinds;
+} allium_bc_desc;
+
+/* InverseAdvectionOperator::InverseAdvectionOperator (src/sweep.cpp:10-244):
+ * builds the upwind graph, its device wavefront levels and assembles the local
+ * matrices.  sigma_t is the piecewise-constant total cross section
+ * [num_groups][num_elements] (a MultiGroupCoefficient sampled per cell).
+ * bc may be NULL (all INFLOW).  Reflective boundaries return
+ * ALLIUM_ERR_UNSUPPORTED. */
+int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe,
+                        const allium_quad_desc* quad, int num_groups,
+                        const double* sigma_t, const allium_bc_desc* bc,
+                        allium_sweep** out);
+
+/* ~InverseAdvectionOperator (src/sweep.cpp:246-257). */
+void allium_sweep_destroy(allium_sweep* s);
+
+/* Use the given cudaStream_t (NULL = the handle's own stream). */
+int allium_sweep_set_stream(allium_sweep* s, void* cuda_stream);
+
+/* Width()/Height() of the operator (src/sweep.cpp:29): psi_size = G*Nw*Ndof. */
+int allium_sweep_sizes(const allium_sweep* s, long long* psi_size, long long* num_dofs,
+                       int* num_levels);
+
+/* AssembleLocalMatrices (src/sweep.cpp:924-1001) after a change of sigma_t
+ * [G][Ne]; as in the reference, the time absorption setting is kept. */
+int allium_sweep_assemble(allium_sweep* s, const double* sigma_t);
+
+/* SetTimeAbsorption (src/sweep.cpp:1003-1022): adds tau * M to every local
+ * system; the time mass matrix is assembled once. */
+int allium_sweep_set_time_absorption(allium_sweep* s, double tau);
+
+/* InverseAdvectionOperator::Mult (src/sweep.cpp:259-669), FP64 throughout,
+ * partially pivoted local LU.  source may equal psi (in-place Mult(psi, psi),
+ * as transport_op.hpp:28 and chive.cpp:733 call it). */
+int allium_sweep_mult(allium_sweep* s, const double* source, double* psi);
+
+/* The same sweep with FP32 storage and FP32 local solves (unpivoted
+ * elimination; the local upwind matrix has a positive definite symmetric part
+ * when sigma_t > 0).  Meant as the inner operator of an FP64 outer iteration. */
+int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi);
+
+/* AdvectionOperator::Mult (src/sweep.cpp:1246-1387): y = L x, FP64. x != y. */
+int allium_sweep_apply_L(allium_sweep* s, const double* x, double* y);
+
+/* AdvectionOperator::ComputeBalance (src/sweep.cpp:1400-1462): absorption +
+ * leakage of psi, written to *out (host or device double). */
+int allium_sweep_balance(allium_sweep* s, const double* psi, double* out);
+
+/* DiscreteToMoment::Mult (src/transport_op.cpp:3-31); num_moments is 1 or dim+1. */
+int allium_sweep_moments(allium_sweep* s, const double* psi, double* phi, int num_moments);
+
+/* DiscreteToMoment::MultTranspose (accumulate = 0) and AddMultTranspose
+ * (accumulate = 1, psi += alpha * D^T phi) (src/transport_op.cpp:33-89). */
+int allium_sweep_moments_transpose(allium_sweep* s, const double* phi, double* psi,
+                                   int num_moments, double alpha, int accumulate);
+
+/* FormTransportSource (src/sweep.cpp:1135-1185) for an isotropic, piecewise
+ * constant source density q_cell [G][Ne] (NULL = 0) and an isotropic inflow
+ * inflow [G][num_attr] indexed by boundary attribute (NULL = vacuum). */
+int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow,
+                             int num_attr, double* source);
+
+/* Isotropic scattering source around the sweep: out = D^T (S phi) + q_fixed,
+ * S = sigma_s [G][Ne] times the MassIntegrator matrix of each cell (within-group
+ * scattering), as chive's source iteration and MomentMethodFixedPointOperator::Mult
+ * build it (src/transport_op.hpp:75-90, exe/chive.cpp:593-599).  q_fixed may be
+ * NULL.  phi is [G][Ndof] (zeroth moment). */
+int allium_sweep_scattering_source(allium_sweep* s, const double* sigma_s, const double* phi,
+                                   const double* q_fixed, double* out);
+
+/* Wavefront level of every (cell, angle) node e*Nw + a (the Kahn frontier
+ * index of src/sweep.cpp:308-512), host or device int array [Ne*Nw]. */
+int allium_sweep_levels(allium_sweep* s, int* levels);
+
+/* Wait for the handle's stream; report sticky kernel errors and clear them. */
+int allium_sweep_synchronize(allium_sweep* s);
+
+const char* allium_sweep_last_error(const allium_sweep* s);
+const char* allium_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ALLIUM_SWEEP_H */

@@ -1,0 +1,264 @@
+"""Parity of the CUDA sweep path with the CPU oracle, through the C ABI.
+
+Tolerances: FP64 results within 1e-12 relative (max-norm over the vector) of
+the oracle; integer levels and the moment sums bit-exact; the FP32 sweep within
+2e-5 relative of the FP64 oracle."""
+import math
+
+import numpy as np
+import pytest
+
+from allium_gb300 import mesh as M
+from allium_gb300 import quadrature as Q
+from allium_gb300._lib import AlliumError
+from allium_gb300.sweep import (AdvectionOperator, DiscreteToMoment, FormTransportSource,
+                                InverseAdvectionOperator, ScatteringSource)
+from oracle.oracle import OracleSweep
+from tests.helpers import mms_phi, mms_source, problem, rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+CASES = [
+    # dim, cells, p, S_N, G, jitter, lump
+    (1, (12,), 0, 4, 2, 0.0, 0),
+    (1, (12,), 1, 4, 2, 0.0, 0),
+    (1, (12,), 2, 4, 1, 0.0, 0),
+    (1, (12,), 3, 4, 1, 0.0, 0),
+    (2, (9, 7), 0, 4, 2, 0.0, 0),
+    (2, (9, 7), 1, 6, 2, 0.0, 0),
+    (2, (9, 7), 2, 4, 1, 0.0, 0),
+    (2, (6, 5), 3, 4, 1, 0.0, 0),
+    (2, (10, 10), 1, 8, 1, 0.2, 0),
+    (2, (8, 8), 2, 6, 1, 0.2, 0),
+    (2, (10, 10), 1, 4, 2, 0.0, 7),
+    (3, (5, 4, 3), 0, 4, 1, 0.0, 0),
+    (3, (5, 4, 3), 1, 4, 2, 0.0, 0),
+    (3, (6, 6, 6), 1, 12, 1, 0.1, 0),
+    (3, (4, 4, 4), 1, 4, 1, 0.0, 7),
+]
+
+
+def build(dim, cells, p, sn, G, jitter, lump, seed=11):
+    mesh, quad, sig = problem(dim, cells, p, sn=sn, G=G, jitter=jitter, seed=seed, lump=lump)
+    return mesh, quad, sig, OracleSweep(mesh, p, quad, sig, lump=lump), InverseAdvectionOperator(mesh, p, quad, sig, lump=lump)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"d{c[0]}p{c[2]}S{c[3]}G{c[4]}j{c[5]}l{c[6]}" for c in CASES])
+def test_sweep_parity(case):
+    mesh, quad, sig, o, L = build(*case)
+    nl, lev_o = o.levels()
+    assert L.num_levels == nl
+    assert np.array_equal(L.levels(), lev_o)
+
+    rng = np.random.default_rng(5)
+    src = rng.random(o.psi_size)
+    ref = o.mult(src)
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert rel_err(psi, ref) < TOL64
+
+    # device pointers, in place
+    d = torch.from_numpy(src).cuda()
+    L.Mult(d, d)
+    L.synchronize()
+    assert np.array_equal(d.cpu().numpy(), psi)
+
+    # FP32 sweep
+    f = torch.from_numpy(src.astype(np.float32)).cuda()
+    L.MultF32(f, f)
+    L.synchronize()
+    assert rel_err(f.cpu().numpy(), ref) < TOL32
+
+    # forward operator and L L^{-1} = I
+    y = np.empty_like(src)
+    AdvectionOperator(L).Mult(src, y)
+    assert rel_err(y, o.apply_L(src)) < TOL64
+    back = np.empty_like(src)
+    L.Mult(y, back)
+    assert np.linalg.norm(back - src) < 1e-12 * max(1.0, np.linalg.norm(src))
+
+    # balance
+    b = AdvectionOperator(L).ComputeBalance(ref)
+    assert abs(b - o.balance(ref)) < TOL64 * abs(o.balance(ref))
+
+
+@pytest.mark.parametrize("case", CASES[:: 2], ids=[f"d{c[0]}p{c[2]}" for c in CASES[:: 2]])
+def test_moments_bit_exact(case):
+    mesh, quad, sig, o, L = build(*case)
+    rng = np.random.default_rng(9)
+    psi = rng.random(o.psi_size)
+    for nmom in (1, mesh.dim + 1):
+        D = DiscreteToMoment(L, nmom)
+        phi = np.empty(D.height)
+        D.Mult(psi, phi)
+        assert np.array_equal(phi, o.moments(psi, nmom))
+        out = np.empty(o.psi_size)
+        D.MultTranspose(phi, out)
+        assert np.array_equal(out, o.moments_transpose(phi, nmom))
+        acc = psi.copy()
+        D.AddMultTranspose(phi, acc, 0.7)
+        assert np.array_equal(acc, o.moments_transpose(phi, nmom, psi=psi.copy(), alpha=0.7, add=True))
+
+
+@pytest.mark.parametrize("case", CASES[1:: 2], ids=[f"d{c[0]}p{c[2]}" for c in CASES[1:: 2]])
+def test_sources(case):
+    mesh, quad, sig, o, L = build(*case)
+    G = sig.shape[0]
+    rng = np.random.default_rng(4)
+    q = rng.random((G, mesh.num_elements))
+    inflow = rng.random((G, 8))
+    assert rel_err(FormTransportSource(L, q, inflow), o.form_source(q_cell=q, inflow=inflow)) < 1e-13
+    phi = rng.random(G * L.ndof)
+    sig_s = rng.random((G, mesh.num_elements))
+    qf = rng.random(o.psi_size)
+    assert rel_err(ScatteringSource(L, sig_s, phi, qf), o.scattering_source(sig_s, phi, qf)) < 1e-13
+
+
+@pytest.mark.parametrize("dim,cells", [(2, (9, 7)), (3, (6, 5, 4))])
+def test_time_absorption(dim, cells):
+    mesh, quad, sig, o, L = build(dim, cells, 1, 4, 2, 0.2, 0)
+    o.set_time_absorption(3.7)
+    L.SetTimeAbsorption(3.7)
+    src = np.random.default_rng(1).random(o.psi_size)
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert rel_err(psi, o.mult(src)) < TOL64
+    y = np.empty_like(src)
+    AdvectionOperator(L).Mult(src, y)
+    assert rel_err(y, o.apply_L(src)) < TOL64
+    # new cross sections (AssembleLocalMatrices) keep the time absorption
+    sig2 = sig * 0.5 + 0.1
+    o2 = OracleSweep(mesh, 1, quad, sig2)
+    o2.set_time_absorption(3.7)
+    L.AssembleLocalMatrices(sig2)
+    L.Mult(src, psi)
+    assert rel_err(psi, o2.mult(src)) < TOL64
+
+
+@pytest.mark.parametrize("dim,cells,p", [(1, (10,), 3), (2, (10, 10), 2), (3, (6, 6, 6), 1), (3, (10, 10, 10), 0)])
+def test_constant_solution(dim, cells, p):
+    # test_sweep.cpp:7-108 on the GPU: sigma = 0, q = 0, unit inflow -> psi == 1
+    mesh = M.cartesian(cells)
+    L = InverseAdvectionOperator(mesh, p, Q.level_symmetric(4, dim), np.zeros((2, mesh.num_elements)))
+    src = FormTransportSource(L, None, np.ones((2, 8)))
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert np.max(np.abs(psi - 1.0)) < 1e-10
+
+
+def _mms_error_gpu(ne, p, lump):
+    mesh = M.cartesian((ne, ne))
+    quad = Q.level_symmetric(6, 2)
+    total, scat = 1.0, 0.25
+    sig = np.full((1, mesh.num_elements), total)
+    o = OracleSweep(mesh, p, quad, sig, lump=lump)   # builds the manufactured source and measures the error
+    src = torch.from_numpy(o.form_source(qfn=mms_source(total, scat),
+                                         inflow_fn=lambda x, om, g, a: 2.0 / 4 / math.pi)).cuda()
+    L = InverseAdvectionOperator(mesh, p, quad, sig, lump=lump)
+    D = DiscreteToMoment(L)
+    sig_s = np.full((1, mesh.num_elements), scat)
+    psi = torch.empty_like(src)
+    phi_old = torch.zeros(L.ndof, dtype=torch.float64, device="cuda")
+    phi = torch.empty_like(phi_old)
+    for _ in range(200):
+        ScatteringSource(L, sig_s, phi_old, src, psi)
+        L.Mult(psi, psi)
+        D.Mult(psi, phi)
+        L.synchronize()
+        norm = torch.linalg.norm(phi_old - phi).item()
+        phi_old.copy_(phi)
+        if norm < 1e-10:
+            break
+    return o.l2_error(phi.cpu().numpy(), 0, 0, mms_phi)
+
+
+@pytest.mark.parametrize("p,lump", [(1, 0), (2, 0), (3, 0), (1, 7)])
+def test_transport_mms_order(p, lump):
+    # test_transport_mms.cpp:89-197 with the GPU sweep inside source iteration
+    e1 = _mms_error_gpu(10, p, lump)
+    e2 = _mms_error_gpu(20, p, lump)
+    assert abs(math.log2(e1 / e2) - (p + 1)) < 0.2
+
+
+def test_chive_2d_workload_parity():
+    # 64 x 64 quads, p = 1, S8 (40 directions), sigma_t = 1, q = 1, vacuum
+    mesh = M.cartesian((64, 64))
+    quad = Q.level_symmetric(8, 2)
+    sig = np.ones((1, mesh.num_elements))
+    o = OracleSweep(mesh, 1, quad, sig)
+    L = InverseAdvectionOperator(mesh, 1, quad, sig)
+    src = FormTransportSource(L, np.ones((1, mesh.num_elements)))
+    assert rel_err(src, o.form_source(q_cell=np.ones((1, mesh.num_elements)))) < 1e-13
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert rel_err(psi, o.mult(src)) < TOL64
+    assert L.num_levels == 127
+
+
+def test_jittered_hex_s12_parity():
+    # the 3D workload's ingredients at 12^3: jittered hexes, S12 (168 directions), log-uniform sigma
+    mesh, quad, sig, o, L = build(3, (12, 12, 12), 1, 12, 1, 0.1, 0, seed=20261203)
+    nl, lev = o.levels()
+    assert np.array_equal(L.levels(), lev)
+    src = np.random.default_rng(2).random(o.psi_size)
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert rel_err(psi, o.mult(src)) < TOL64
+
+
+def test_full_size_3d_properties():
+    # 64^3 jittered hexes, p = 1, S12: size-independent checks at full size.
+    mesh, quad, sig = problem(3, (64, 64, 64), 1, sn=12, G=1, jitter=0.1, seed=20261203)
+    L = InverseAdvectionOperator(mesh, 1, quad, sig)
+    n = L.width
+    q = torch.from_numpy(FormTransportSource(L, np.random.default_rng(3).random((1, mesh.num_elements)))).cuda()
+    psi = torch.empty_like(q)
+    L.Mult(q, psi)
+    y = torch.empty_like(q)
+    AdvectionOperator(L).Mult(psi, y)
+    L.synchronize()
+    # L (L^{-1} q) = q
+    assert (torch.linalg.norm(y - q) / torch.linalg.norm(q)).item() < 1e-12
+    # vacuum balance: absorption + leakage = total source
+    total = float((q.view(quad.size, -1).sum(1).cpu().numpy() * quad.weights).sum())
+    bal = AdvectionOperator(L).ComputeBalance(psi)
+    assert abs(bal - total) < 1e-11 * abs(total)
+    # FP32 sweep against the FP64 sweep
+    f = q.float()
+    L.MultF32(f, f)
+    L.synchronize()
+    assert (torch.max(torch.abs(f.double() - psi)) / torch.max(torch.abs(psi))).item() < TOL32
+    del q, psi, y, f
+    assert n == 64 ** 3 * 8 * 168
+
+
+def test_cycle_is_reported():
+    # +-0.2h jitter with S12's grazing directions gives a cyclic upwind graph;
+    # the reference aborts (sweep.cpp:205-208), the library returns NOT_DAG
+    mesh, quad, sig = problem(3, (16, 16, 16), 1, sn=12, jitter=0.2, seed=20261203)
+    assert OracleSweep(mesh, 1, quad, sig).levels()[0] == -1
+    with pytest.raises(AlliumError) as e:
+        InverseAdvectionOperator(mesh, 1, quad, sig)
+    assert e.value.status == 2
+
+
+def test_errors_are_reported():
+    mesh, quad, sig = problem(2, (4, 4), 1)
+    with pytest.raises(AlliumError) as e:
+        InverseAdvectionOperator(mesh, 1, quad, sig, bc={1: "reflective"})
+    assert e.value.status == 7
+    m3, q3, s3 = problem(3, (2, 2, 2), 2)
+    with pytest.raises(AlliumError) as e:
+        InverseAdvectionOperator(m3, 2, q3, s3)
+    assert e.value.status == 7
+    L = InverseAdvectionOperator(mesh, 1, quad, sig)
+    x = np.zeros(L.width)
+    with pytest.raises(AlliumError) as e:
+        AdvectionOperator(L).Mult(x, x)
+    assert e.value.status == 1
+    with pytest.raises(ValueError):
+        L.Mult(np.zeros(3), np.zeros(3))

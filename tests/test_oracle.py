@@ -1,0 +1,170 @@
+"""Pins the CPU oracle against the reference's own known answers and identities
+(test/test_integrators.cpp, test/test_sweep.cpp, test/test_transport_mms.cpp,
+test/test_angle_quad.cpp).  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+from allium_gb300 import mesh as M
+from allium_gb300 import quadrature as Q
+from oracle.oracle import OracleSweep
+from tests.helpers import mms_phi, mms_source, problem
+
+
+@pytest.mark.parametrize("lump", [0, 7])
+def test_face_blocks_known_answer(lump):
+    # test_integrators.cpp:269-347: 2x1 quads, p = 1 Lobatto, interior face x = 1/2
+    mesh = M.cartesian((2, 1))
+    o = OracleSweep(mesh, 1, Q.level_symmetric(4, 2), np.ones((1, 2)), lump=lump)
+    faces = [f for f in range(o.num_faces()) if o.face_info(f)[0][2] >= 0]
+    assert len(faces) == 1
+    F = o.face_matrices(faces[0])
+    a, b = (0.5, 0.0) if lump else (1.0 / 3, 1.0 / 6)
+    ex11 = np.zeros((4, 4)); ex11[1, 1] = ex11[3, 3] = a; ex11[1, 3] = ex11[3, 1] = b
+    ex12 = np.zeros((4, 4)); ex12[1, 0] = ex12[3, 2] = a; ex12[1, 2] = ex12[3, 0] = b
+    ex22 = np.zeros((4, 4)); ex22[0, 0] = ex22[2, 2] = a; ex22[0, 2] = ex22[2, 0] = b
+    assert np.linalg.norm(F[0, 0] - ex11) < 1e-14
+    assert np.linalg.norm(F[0, 1] - ex12) < 1e-14
+    assert np.linalg.norm(F[1, 0].T - F[0, 1]) < 1e-14
+    assert np.linalg.norm(F[1, 1] - ex22) < 1e-14
+
+
+CONST_CASES = [(1, (10,), 0, 0), (1, (10,), 1, 0), (1, (10,), 1, 7), (1, (10,), 2, 0), (1, (10,), 3, 0),
+               (2, (10, 10), 0, 0), (2, (10, 10), 1, 0), (2, (10, 10), 1, 7), (2, (10, 10), 2, 0),
+               (3, (10, 10, 10), 0, 0), (3, (6, 6, 6), 1, 0), (3, (6, 6, 6), 1, 7), (3, (3, 3, 3), 2, 0)]
+
+
+@pytest.mark.parametrize("dim,cells,p,lump", CONST_CASES)
+def test_constant_solution(dim, cells, p, lump):
+    # test_sweep.cpp:7-108: sigma = 0, q = 0, unit inflow everywhere -> psi == 1
+    mesh = M.cartesian(cells)
+    quad = Q.level_symmetric(4, dim)
+    o = OracleSweep(mesh, p, quad, np.zeros((2, mesh.num_elements)), lump=lump)
+    src = o.form_source(inflow=np.ones((2, 8)))
+    psi = o.mult(src)
+    assert np.max(np.abs(psi - 1.0)) < 1e-10
+
+
+@pytest.mark.parametrize("dim,cells,lump", [(1, (10,), 0), (2, (3, 3), 0), (3, (3, 3, 3), 0),
+                                            (1, (10,), 7), (2, (3, 3), 7), (3, (3, 3, 3), 7)])
+def test_L_Linv_identity(dim, cells, lump):
+    # test_sweep.cpp:289-361: || L^{-1} (L x) - x || < 1e-12, sigma = (1, 0.5)
+    mesh = M.cartesian(cells)
+    quad = Q.level_symmetric(4, dim)
+    sig = np.array([[1.0], [0.5]]) * np.ones((2, mesh.num_elements))
+    o = OracleSweep(mesh, 1, quad, sig, lump=lump)
+    x = np.random.default_rng(12345).random(o.psi_size)
+    psi = o.mult(o.apply_L(x))
+    assert np.linalg.norm(psi - x) < 1e-12
+
+
+def _exp_error(cells, p, exact, lump=0):
+    mesh = M.cartesian(cells)
+    dim = mesh.dim
+    quad = Q.single_angle(Q.level_symmetric(4, dim), 0)
+    sig = np.array([[1.0], [0.5]]) * np.ones((2, mesh.num_elements))
+    o = OracleSweep(mesh, p, quad, sig, lump=lump)
+    src = o.form_source(inflow=np.ones((2, 8)))
+    psi = o.mult(src)
+    return sum(o.l2_error(psi, g, 0, lambda x, om, gg: exact(sig[gg, 0], x, om)) for g in range(2))
+
+
+def _exp1(alpha, x, om):
+    return math.exp(-x[0] / om[0] * alpha)
+
+
+def _exp2(alpha, x, om):
+    return math.exp(-x[1] / om[0] * alpha) if x[0] > x[1] else math.exp(-x[0] / om[1] * alpha)
+
+
+@pytest.mark.parametrize("p,lump", [(1, 0), (1, 7), (2, 0), (3, 0)])
+def test_exponential_order_1d(p, lump):
+    # test_sweep.cpp:178-220: order p + 1 in 1D
+    e1 = _exp_error((10,), p, _exp1, lump)
+    e2 = _exp_error((20,), p, _exp1, lump)
+    assert abs(math.log2(e1 / e2) - (p + 1)) < 0.1
+
+
+def test_exponential_order_2d():
+    # test_sweep.cpp:222-230: discontinuity not mesh aligned -> order ~1
+    e1 = _exp_error((50, 50), 1, _exp2)
+    e2 = _exp_error((100, 100), 1, _exp2)
+    assert abs(math.log2(e1 / e2) - 1.0) < 0.2
+
+
+def _mms_error(ne, p, lump):
+    mesh = M.cartesian((ne, ne))
+    quad = Q.level_symmetric(6, 2)
+    total, scat = 1.0, 0.25
+    o = OracleSweep(mesh, p, quad, np.full((1, mesh.num_elements), total), lump=lump)
+    src = o.form_source(qfn=mms_source(total, scat), inflow_fn=lambda x, om, g, a: 2.0 / 4 / math.pi)
+    sig_s = np.full((1, mesh.num_elements), scat)
+    phi_old = np.zeros(o.ndof)
+    for _ in range(200):
+        psi = o.scattering_source(sig_s, phi_old, src)
+        o.mult(psi, psi)
+        phi = o.moments(psi)
+        norm = np.linalg.norm(phi_old - phi)
+        phi_old = phi
+        if norm < 1e-10:
+            break
+    return o.l2_error(phi, 0, 0, mms_phi)
+
+
+@pytest.mark.parametrize("p,lump", [(1, 0), (2, 0), (3, 0), (1, 7)])
+def test_transport_mms_order(p, lump):
+    # test_transport_mms.cpp:89-197: source iteration, L2 order p + 1 +- 0.2
+    e1 = _mms_error(10, p, lump)
+    e2 = _mms_error(20, p, lump)
+    assert abs(math.log2(e1 / e2) - (p + 1)) < 0.2
+
+
+def test_moments_known_answers():
+    # test_angle_quad.cpp:86-123 on one DOF: D of a quadratic and a linear psi
+    mesh = M.cartesian((1,) * 2)
+    quad = Q.level_symmetric(4, 2)
+    o = OracleSweep(mesh, 0, quad, np.ones((1, 1)))
+    om = quad.omega
+    psi = 2 * om[:, 0] ** 2 + om[:, 1] ** 2 + om[:, 0] * om[:, 1]
+    assert abs(o.moments(psi)[0] - 4 * math.pi) < 1e-13
+    psi = ((om ** 2).sum(1) + om[:, 0] + om[:, 1]) / 4 / math.pi
+    phi = o.moments(psi, nmom=3)
+    assert abs(phi[0] - 2.0 / 3) < 1e-13 and abs(phi[1] - 1.0 / 3) < 1e-13 and abs(phi[2] - 1.0 / 3) < 1e-13
+
+
+def test_levels_structured():
+    # on a structured grid the Kahn frontier of (cell i,j) in an octant is i + j
+    mesh, quad, sig = problem(2, (7, 5), 1)
+    o = OracleSweep(mesh, 1, quad, sig)
+    nl, lev = o.levels()
+    assert nl == 7 + 5 - 1
+    lev = lev.reshape(mesh.num_elements, quad.size)
+    for a in range(quad.size):
+        sx, sy = np.sign(quad.omega[a])
+        for e in range(mesh.num_elements):
+            i, j = e % 7, e // 7
+            ii = i if sx > 0 else 6 - i
+            jj = j if sy > 0 else 4 - j
+            assert lev[e, a] == ii + jj
+
+
+def test_balance_vacuum():
+    # with vacuum boundaries and no scattering, absorption + leakage of L^{-1} q
+    # equals the total source sum_a w_a sum_i q(a, i)
+    mesh, quad, sig = problem(2, (6, 6), 1, jitter=0.2, G=2)
+    o = OracleSweep(mesh, 1, quad, sig)
+    src = o.form_source(q_cell=np.ones((2, mesh.num_elements)))
+    psi = o.mult(src)
+    total = sum(quad.weights[a] * src.reshape(2, quad.size, -1)[g, a].sum() for g in range(2) for a in range(quad.size))
+    assert abs(o.balance(psi) - total) < 1e-12 * abs(total)
+
+
+def test_in_place_and_threads():
+    mesh, quad, sig = problem(3, (4, 4, 4), 1, jitter=0.2)
+    o = OracleSweep(mesh, 1, quad, sig)
+    x = np.random.default_rng(3).random(o.psi_size)
+    a = o.mult(x, threads=1)
+    b = x.copy()
+    o.mult(b, b, threads=4)
+    assert np.array_equal(a, b)
