@@ -113,15 +113,10 @@ class InverseAdvectionOperator:
         """psi = L^{-1} source (FP64); source may be psi itself."""
         sp = _ptr(source, np.float64, self.width, "source")
         pp = _ptr(psi, np.float64, self.height, "psi")
-        sweeps = self.num_pbj_sweeps if self.pbj else 1
-        if sweeps > 1 and sp == pp:
-            # the reference keeps a copy of the source when it sweeps more than once
-            source = source.copy() if isinstance(source, np.ndarray) else source.clone()
-            sp = _ptr(source, np.float64, self.width, "source")
-        for _ in range(sweeps):
-            # on one GPU the block Jacobi sweep has no off-rank data to lag and
-            # is the upwind sweep itself
-            check(_lib.lib().allium_sweep_mult(self.h, C.c_void_p(sp), C.c_void_p(pp)), self.h)
+        # With one GPU owning every cell, the parallel block Jacobi variant
+        # (sweep.cpp:671-875) has no off-rank data to lag: any number of PBJ
+        # sweeps gives the upwind result, so one sweep serves both modes.
+        check(_lib.lib().allium_sweep_mult(self.h, C.c_void_p(sp), C.c_void_p(pp)), self.h)
 
     def MultF32(self, source, psi):
         """FP32 sweep (storage and local solves in FP32)."""

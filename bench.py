@@ -43,10 +43,10 @@ METRIC = "swept cell-angle-group DOF/s"
 UNIT = "DOF*angle*group/s"
 
 
-def workload():
+def workload(cells=CELLS):
     from allium_gb300 import mesh as M
     from allium_gb300 import quadrature as Q
-    mesh = M.cartesian(CELLS, jitter=JITTER, seed=SEED)
+    mesh = M.cartesian(cells, jitter=JITTER, seed=SEED)
     quad = Q.level_symmetric(SN, 3)
     rng = np.random.default_rng(SEED + 1)
     sigma = 10.0 ** rng.uniform(-1.0, 2.0, size=(1, mesh.num_elements))
@@ -54,7 +54,9 @@ def workload():
     return mesh, quad, sigma, q
 
 
-def config(levels=None):
+def config(levels=None, cells=CELLS):
+    if tuple(cells) != CELLS:
+        return {"workload": f"profiling case: {cells[0]}^3 jittered hex mesh, p=1, S12, 1 group", "levels": levels}
     c = {"workload": "chive 3D sweep: 64^3 hex mesh of [0,1]^3, interior vertices jittered +-0.1h (seed 20261203; +-0.2h gives a cyclic S12 upwind graph), "
                      "p=1 Gauss-Lobatto DG (8 DOF/cell), level-symmetric S12 (168 directions), 1 group, "
                      "sigma_t log-uniform [0.1,100] per cell, vacuum boundaries, q ~ U[0,1] per cell",
@@ -191,7 +193,8 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    mesh, quad, sigma, q = workload()
+    cells = (args.cells,) * 3
+    mesh, quad, sigma, q = workload(cells)
     L = InverseAdvectionOperator(mesh, ORDER, quad, sigma)
     stream = torch.cuda.current_stream()
     N = L.width
@@ -210,12 +213,12 @@ def run_gpu(args):
     L.synchronize()
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            L.Mult(src, psi)
-        ev1.record(stream)
-        L.synchronize()
+    clk = ClockSampler(local).__enter__()   # sampled across all timed regions below
+    ev0.record(stream)
+    for _ in range(args.steps):
+        L.Mult(src, psi)
+    ev1.record(stream)
+    L.synchronize()
     barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
     if dist:
@@ -253,6 +256,7 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = world * N / e2e_s
+    clk.__exit__(None, None, None)
     assert torch.equal(h_psi, psi.cpu()), "host and device paths disagree"
 
     if rank != 0:
@@ -273,7 +277,7 @@ def run_gpu(args):
     fp64_flops = 2 * 590.0 * N / 8
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(L.num_levels),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(L.num_levels, cells),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
                     "ms_per_step": e2e_s * 1e3},
             "gpu_launches": args.steps * L.num_levels,
@@ -283,7 +287,7 @@ def run_gpu(args):
                      "max_rel_err_vs_fp64": err32,
                      "roofline_frac": (8.0 * N / (ms32 * 1e-3) / 1e9) / peak},
             "clocks": clk.summary()}
-    if not args.no_cpu:
+    if not args.no_cpu and tuple(cells) == CELLS:
         rates, size = cpu_sweep_sample(os.cpu_count() or 1, 3, 1)
         line["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": os.cpu_count(),
                                 "kind": "port",
@@ -296,10 +300,11 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cells", type=int, default=CELLS[0], help="cells per axis (smaller cases for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
