@@ -44,6 +44,7 @@ EXPORTS = {
     "allium_sweep_assemble": (C.c_int, [C.c_void_p, C.c_void_p]),
     "allium_sweep_set_time_absorption": (C.c_int, [C.c_void_p, C.c_double]),
     "allium_sweep_mult": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_set_factor_cache": (C.c_int, [C.c_void_p, C.c_int]),
     "allium_sweep_mult_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_apply_L": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -1,14 +1,11 @@
 // C ABI of liballium_sweep.so (declared in include/allium_sweep.h).
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "internal.h"
-
-struct allium_sweep {
-    allium::Handle h;
-};
 
 using allium::Handle;
 
@@ -61,9 +58,11 @@ int check_status(Handle& h) {
 }
 
 void free_all(Handle& h) {
-    void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
+    allium::drop_graphs(h);
+    if (h.capture_stream) cudaStreamDestroy(h.capture_stream);
+    void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
-                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch};
+                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -108,7 +107,7 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     if (fe->order < 0 || fe->order > allium::kMaxOrder || fe->basis != ALLIUM_BASIS_GAUSS_LOBATTO ||
         fe->lump < 0 || fe->lump > 7)
         return ALLIUM_ERR_UNSUPPORTED;
-    if (mesh->dim == 3 && fe->order > 1) return ALLIUM_ERR_UNSUPPORTED;
+    if (mesh->dim == 3 && fe->order > 2) return ALLIUM_ERR_UNSUPPORTED;   // 64 x 64 local systems
     if (bc)
         for (int i = 0; i < bc->num; ++i)
             if (bc->kinds[i] != ALLIUM_BC_INFLOW) return ALLIUM_ERR_UNSUPPORTED;
@@ -155,6 +154,8 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     STEP(upload(h, topo.nbrmap.data(), topo.nbrmap.size(), &h.d_nbrmap));
     STEP(upload(h, sigma_t, (size_t)h.G * h.ne, &h.d_sigma));
     CSTEP(cudaMalloc(&h.d_normals, (size_t)h.nfaces * h.dim * sizeof(double)));
+    CSTEP(cudaMalloc(&h.d_dots, (size_t)h.nfaces * h.Nw * sizeof(double)));
+    CSTEP(cudaMalloc(&h.f_dots, (size_t)h.nfaces * h.Nw * sizeof(float)));
     CSTEP(cudaMalloc(&h.d_G, (size_t)h.ne * h.dim * nn * sizeof(double)));
     CSTEP(cudaMalloc(&h.d_M, (size_t)h.ne * nn * sizeof(double)));
     CSTEP(cudaMalloc(&h.d_F, (size_t)h.ne * h.nface * h.nf * h.nf * sizeof(double)));
@@ -165,6 +166,7 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     h.scratch_len = 4096;
     CSTEP(cudaMalloc(&h.d_scratch, (h.scratch_len + 1) * sizeof(double)));
     CSTEP(allium::launch_face_normals(h));
+    CSTEP(allium::launch_face_dots(h));
     CSTEP(allium::launch_assemble(h));
     STEP(allium::compute_levels(h));
     CSTEP(cudaStreamSynchronize(h.stream));
@@ -184,13 +186,6 @@ void allium_sweep_destroy(allium_sweep* s) {
 int allium_sweep_set_stream(allium_sweep* s, void* stream) {
     if (!s) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
-    if (!stream) {
-        if (!h.own_stream) {
-            CUDA_OR_FAIL(h, cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
-            h.own_stream = true;
-        }
-        return ALLIUM_OK;
-    }
     if (h.own_stream) {
         CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
         cudaStreamDestroy(h.stream);
@@ -213,6 +208,7 @@ int allium_sweep_assemble(allium_sweep* s, const double* sigma_t) {
     Handle& h = s->h;
     int st = upload(h, sigma_t, (size_t)h.G * h.ne, &h.d_sigma);
     if (st) return st;
+    h.inv_valid = false;
     st = refresh_fp32(h);
     if (st) return st;
     CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
@@ -230,7 +226,11 @@ static int ensure_mass2(Handle& h) {
 int allium_sweep_set_time_absorption(allium_sweep* s, double tau) {
     if (!s) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
+    if (tau != h.tau || !h.time_dependent) h.inv_valid = false;
     h.tau = tau;
+    // captured launches carry tau and the time-mass pointers as arguments
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    allium::drop_graphs(h);
     if (!h.time_dependent) {
         int st = ensure_mass2(h);
         if (st) return st;
@@ -271,10 +271,28 @@ int allium_sweep_scattering_source(allium_sweep* s, const double* sigma_s, const
     return ALLIUM_OK;
 }
 
+static bool misaligned(const void* a, const void* b, bool da, bool db) {
+    return (da && ((uintptr_t)a & 15)) || (db && ((uintptr_t)b & 15));
+}
+
+// Allocate the FP64 factor cache when enabled, supported and it leaves at
+// least half of the free device memory untouched; otherwise sweep without it.
+static void prepare_factor_cache(Handle& h) {
+    if (h.d_inv || h.factor_cache == 0 || !allium::factor_cache_supported(h)) return;
+    const size_t need = (size_t)h.G * h.ne * h.Nw * h.n * h.n * sizeof(double);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return; }
+    if (need > free_b / 2) return;
+    if (cudaMalloc(&h.d_inv, need) != cudaSuccess) { cudaGetLastError(); h.d_inv = nullptr; return; }
+    h.inv_valid = false;
+}
+
 int allium_sweep_mult(allium_sweep* s, const double* source, double* psi) {
     if (!s || !source || !psi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
+    prepare_factor_cache(h);
     const bool ds = on_device(source), dp = on_device(psi);
+    if (misaligned(source, psi, ds, dp)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
     if (ds && dp) {
         CUDA_OR_FAIL(h, allium::launch_sweep_fp64(h, source, psi));
         return ALLIUM_OK;
@@ -297,6 +315,7 @@ int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi) {
     Handle& h = s->h;
     if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
     const bool ds = on_device(source), dp = on_device(psi);
+    if (misaligned(source, psi, ds, dp)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
     if (ds && dp) {
         CUDA_OR_FAIL(h, allium::launch_sweep_fp32(h, source, psi));
         return ALLIUM_OK;
@@ -439,6 +458,20 @@ int allium_sweep_levels(allium_sweep* s, int* levels) {
     Handle& h = s->h;
     CUDA_OR_FAIL(h, cudaMemcpyAsync(levels, h.d_level, (size_t)h.ne * h.Nw * sizeof(int), cudaMemcpyDefault, h.stream));
     CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_set_factor_cache(allium_sweep* s, int mode) {
+    if (!s || mode < 0 || mode > 1) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    h.factor_cache = mode;
+    if (mode == 0 && h.d_inv) {
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+        allium::drop_graphs(h);
+        cudaFree(h.d_inv);
+        h.d_inv = nullptr;
+        h.inv_valid = false;
+    }
     return ALLIUM_OK;
 }
 

@@ -31,15 +31,6 @@ struct Slot {
     int face, nbr, side, attr;
 };
 
-struct SweepArgsBase {
-    int ne, Nw, G, dim;
-    long long ndof;
-    const double* omega;     // [Nw][dim]
-    const double* normals;   // [nfaces][dim] unit, out of element 1
-    const Slot* slots;       // [ne][2 dim]
-    const uint8_t* nbrmap;   // [ne][2 dim][nf] nbr local DOF of each self face DOF
-};
-
 struct Handle {
     // problem description
     int dim = 0, p = 0, n = 0, nf = 0, nface = 0, ne = 0, Nw = 0, G = 0, lump = 0;
@@ -58,6 +49,10 @@ struct Handle {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     double *d_omega = nullptr, *d_weights = nullptr, *d_corners = nullptr, *d_normals = nullptr;
+    // Omega_a . n_f for every face and angle, [nfaces][Nw] (n_f out of element 1);
+    // the single source of every upwind decision (graph, levels, sweep, L)
+    double* d_dots = nullptr;
+    float* f_dots = nullptr;         // FP32 copy with the sign of the FP64 value
     Slot* d_slots = nullptr;
     int* d_face_e1k1 = nullptr;      // [nfaces][2]
     uint8_t* d_nbrmap = nullptr;
@@ -71,9 +66,64 @@ struct Handle {
     double* d_scratch = nullptr;     // reduction partials
     size_t scratch_len = 0;
     bool fp32_ready = false;
+    // FP64 factor cache: inverse of every local matrix, entry-major over the
+    // level-sorted node-group order (allocated on the first FP64 Mult when it fits)
+    int factor_cache = 1;            // 0 off, 1 automatic
+    double* d_inv = nullptr;
+    bool inv_valid = false;
+
+    // CUDA graphs of the per-level launch sequence, keyed by kind and vectors
+    struct GraphEntry {
+        int kind = -1;
+        const void* src = nullptr;
+        void* dst = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    };
+    static constexpr int kGraphSlots = 8;
+    GraphEntry graphs[kGraphSlots];
+    int graph_next = 0;
+    cudaStream_t capture_stream = nullptr;
+    bool use_graphs = true;
 
     std::string last_error;
 };
+
+// Launch `body(stream)` through a cached CUDA graph keyed by (kind, src, dst):
+// captured once on a private stream, replayed on h.stream afterwards.
+template <typename Body>
+cudaError_t run_graph(Handle& h, int kind, const void* src, void* dst, Body&& body) {
+    if (!h.use_graphs) return body(h.stream);
+    for (auto& g : h.graphs)
+        if (g.exec && g.kind == kind && g.src == src && g.dst == dst) return cudaGraphLaunch(g.exec, h.stream);
+    cudaError_t e = cudaSuccess;
+    if (!h.capture_stream) {
+        e = cudaStreamCreateWithFlags(&h.capture_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaStreamBeginCapture(h.capture_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t be = body(h.capture_stream);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(h.capture_stream, &graph);
+    if (be != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return be; }
+    if (e != cudaSuccess) return e;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return e;
+    auto& slot = h.graphs[h.graph_next];
+    h.graph_next = (h.graph_next + 1) % Handle::kGraphSlots;
+    if (slot.exec) cudaGraphExecDestroy(slot.exec);
+    slot.kind = kind; slot.src = src; slot.dst = dst; slot.exec = exec;
+    return cudaGraphLaunch(exec, h.stream);
+}
+
+inline void drop_graphs(Handle& h) {
+    for (auto& g : h.graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = Handle::GraphEntry{};
+    }
+}
 
 // kernel error bits (d_status)
 constexpr int kErrSingular = 1;
@@ -91,6 +141,7 @@ int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string&
 
 // ---- setup kernels (setup.cu)
 cudaError_t launch_face_normals(Handle& h);
+cudaError_t launch_face_dots(Handle& h);
 cudaError_t launch_assemble(Handle& h);
 cudaError_t launch_time_mass(Handle& h);
 int compute_levels(Handle& h);   // returns an allium status
@@ -107,5 +158,11 @@ RefTables make_ref_tables(int dim, int p, int lump);
 cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi);
 cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi);
 cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y);
+bool factor_cache_supported(const Handle& h);
 
 }  // namespace allium
+
+// the opaque handle behind the C ABI
+struct allium_sweep {
+    allium::Handle h;
+};

@@ -131,6 +131,31 @@ cudaError_t launch_face_normals(Handle& h) {
     return cudaGetLastError();
 }
 
+// Omega_a . n_f for all (face, angle), rounded exactly as written (no FMA).
+// The FP32 copy keeps the sign of the FP64 value even where it would round to
+// zero, so FP32 and FP64 sweeps take the same upwind decisions.
+__global__ void k_face_dots(int nfaces, int Nw, int dim, const double* __restrict__ omega,
+                            const double* __restrict__ normals, double* __restrict__ dots, float* __restrict__ fdots) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nfaces * Nw) return;
+    const int f = (int)(t / Nw), a = (int)(t % Nw);
+    double om[3] = {0, 0, 0}, nr[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) { om[d] = omega[a * dim + d]; nr[d] = normals[(size_t)f * dim + d]; }
+    const double v = dot_exact(dim, om, nr);
+    float fv = (float)v;
+    if (fv == 0.0f && v != 0.0) fv = v > 0.0 ? 1.401298464e-45f : -1.401298464e-45f;
+    dots[t] = v;
+    fdots[t] = fv;
+}
+
+cudaError_t launch_face_dots(Handle& h) {
+    const long long total = (long long)h.nfaces * h.Nw;
+    const int b = 256;
+    k_face_dots<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.nfaces, h.Nw, h.dim, h.d_omega, h.d_normals,
+                                                                      h.d_dots, h.f_dots);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ assembly
 // One block per cell.  Geometric factors of each quadrature point are staged
 // in shared memory, then the threads share out the matrix entries.
@@ -276,24 +301,21 @@ cudaError_t launch_time_mass(Handle& h) {
 // ------------------------------------------------------------ levels
 // Edge rule of sweep.cpp:157-175 on one face: element 1 -> element 2 unless
 // Omega . n_face < 0 (n_face points out of element 1).
-__device__ inline bool forward_edge(int dim, const double* om, const double* nr) {
-    return !(dot_exact(dim, om, nr) < 0.0);
+__device__ inline bool forward_edge(const double* __restrict__ dots, int Nw, int face, int a) {
+    return !(dots[(size_t)face * Nw + a] < 0.0);
 }
 
-__global__ void k_indegree(int ne, int Nw, int dim, const double* __restrict__ omega,
-                           const double* __restrict__ normals, const Slot* __restrict__ slots,
+__global__ void k_indegree(int ne, int Nw, int dim, const double* __restrict__ dots, const Slot* __restrict__ slots,
                            int* __restrict__ indeg, int* __restrict__ level,
                            int* __restrict__ frontier, int* __restrict__ fcount) {
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= (long long)ne * Nw) return;
     const int e = (int)(v / Nw), a = (int)(v % Nw), nface = 2 * dim;
-    double om[3] = {0, 0, 0};
-    for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
     int c = 0;
     for (int k = 0; k < nface; ++k) {
         const Slot s = slots[(size_t)e * nface + k];
         if (s.nbr < 0) continue;
-        const bool fwd = forward_edge(dim, om, normals + (size_t)s.face * dim);
+        const bool fwd = forward_edge(dots, Nw, s.face, a);
         if (s.side ? fwd : !fwd) ++c;
     }
     indeg[v] = c;
@@ -303,7 +325,7 @@ __global__ void k_indegree(int ne, int Nw, int dim, const double* __restrict__ o
     }
 }
 
-__global__ void k_kahn(int Nw, int dim, const double* __restrict__ omega, const double* __restrict__ normals,
+__global__ void k_kahn(int Nw, int dim, const double* __restrict__ dots,
                        const Slot* __restrict__ slots, int* __restrict__ indeg, int* __restrict__ level,
                        const int* __restrict__ cur, int ncur, int* __restrict__ next, int* __restrict__ ncount,
                        int lev) {
@@ -311,12 +333,10 @@ __global__ void k_kahn(int Nw, int dim, const double* __restrict__ omega, const 
     if (t >= ncur) return;
     const int u = cur[t];
     const int e = u / Nw, a = u % Nw, nface = 2 * dim;
-    double om[3] = {0, 0, 0};
-    for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
     for (int k = 0; k < nface; ++k) {
         const Slot s = slots[(size_t)e * nface + k];
         if (s.nbr < 0) continue;
-        const bool fwd = forward_edge(dim, om, normals + (size_t)s.face * dim);
+        const bool fwd = forward_edge(dots, Nw, s.face, a);
         if (!(s.side ? !fwd : fwd)) continue;   // not an out-edge of u
         const int v = s.nbr * Nw + a;
         if (atomicSub(&indeg[v], 1) == 1) {
@@ -349,7 +369,7 @@ int compute_levels(Handle& h) {
     CK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(int), h.stream));
     const int b = 256;
     const unsigned gN = (unsigned)((N + b - 1) / b);
-    k_indegree<<<gN, b, 0, h.stream>>>(h.ne, h.Nw, h.dim, h.d_omega, h.d_normals, h.d_slots, d_indeg, h.d_level, d_fa, d_cnt);
+    k_indegree<<<gN, b, 0, h.stream>>>(h.ne, h.Nw, h.dim, h.d_dots, h.d_slots, d_indeg, h.d_level, d_fa, d_cnt);
     CK(cudaGetLastError());
     int ncur = 0;
     CK(cudaMemcpyAsync(&ncur, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
@@ -359,7 +379,7 @@ int compute_levels(Handle& h) {
     while (ncur > 0) {
         done += ncur;
         CK(cudaMemsetAsync(d_cnt + 1, 0, sizeof(int), h.stream));
-        k_kahn<<<(ncur + b - 1) / b, b, 0, h.stream>>>(h.Nw, h.dim, h.d_omega, h.d_normals, h.d_slots, d_indeg,
+        k_kahn<<<(ncur + b - 1) / b, b, 0, h.stream>>>(h.Nw, h.dim, h.d_dots, h.d_slots, d_indeg,
                                                         h.d_level, d_fa, ncur, d_fb, d_cnt + 1, lev);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&ncur, d_cnt + 1, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
@@ -554,8 +574,8 @@ cudaError_t launch_moments_transpose(Handle& h, const double* phi, double* psi, 
 constexpr int kBalanceBlock = 256;
 
 __global__ void __launch_bounds__(kBalanceBlock) k_balance(RefTables t, int ne, int Nw, int G, long long ndof,
-                                                           const double* __restrict__ omega, const double* __restrict__ w,
-                                                           const double* __restrict__ normals, const Slot* __restrict__ slots,
+                                                           const double* __restrict__ w,
+                                                           const double* __restrict__ dots, const Slot* __restrict__ slots,
                                                            const double* __restrict__ M, const double* __restrict__ Mt,
                                                            const double* __restrict__ F, const double* __restrict__ sigma,
                                                            double tau, int td, const double* __restrict__ psi,
@@ -582,12 +602,10 @@ __global__ void __launch_bounds__(kBalanceBlock) k_balance(RefTables t, int ne, 
             absb += s;
         }
         double contrib = absb * w[a];
-        double om[3] = {0, 0, 0};
-        for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
         for (int k = 0; k < nface; ++k) {
             const Slot s = slots[(size_t)e * nface + k];
             if (s.nbr >= 0) continue;
-            const double dot = dot_exact(dim, om, normals + (size_t)s.face * dim);
+            const double dot = dots[(size_t)s.face * Nw + a];
             if (dot < 0.0) continue;
             const double* Fk = F + ((size_t)e * nface + k) * nf * nf;
             double sum = 0.0;
@@ -628,7 +646,7 @@ cudaError_t launch_balance(Handle& h, const double* psi, double* partial, int nb
     long long want = (total + kBalanceBlock - 1) / kBalanceBlock;
     const int nb = (int)(want < nblocks_max ? want : nblocks_max);
     *nblocks = nb < 1 ? 1 : nb;
-    k_balance<<<*nblocks, kBalanceBlock, 0, h.stream>>>(h.ref, h.ne, h.Nw, h.G, h.ndof, h.d_omega, h.d_weights, h.d_normals,
+    k_balance<<<*nblocks, kBalanceBlock, 0, h.stream>>>(h.ref, h.ne, h.Nw, h.G, h.ndof, h.d_weights, h.d_dots,
                                                          h.d_slots, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.tau,
                                                          h.time_dependent ? 1 : 0, psi, partial);
     return cudaGetLastError();

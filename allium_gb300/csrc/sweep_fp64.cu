@@ -6,12 +6,29 @@ namespace allium {
 cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
     SweepArgs<double> a;
     a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
-    a.omega = h.d_omega; a.normals = h.d_normals; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
+    a.omega = h.d_omega; a.dots = h.d_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
     a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
     a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status;
-    return sweep_dispatch<double, true>(h, a);
+    if (h.d_inv) {
+        const int mode = h.inv_valid ? 2 : 1;
+        auto body = [&](cudaStream_t st) -> cudaError_t {
+            switch (h.dim * 10 + h.p) {
+                case 11: return sweep_levels_inv<1, 1>(h, a, mode, st);
+                case 21: return sweep_levels_inv<2, 1>(h, a, mode, st);
+                case 31: return sweep_levels_inv<3, 1>(h, a, mode, st);
+                default: return cudaErrorNotSupported;
+            }
+        };
+        // the factor pass runs once per operator: launch it directly
+        cudaError_t e = (mode == 1) ? body(h.stream) : run_graph(h, 2, src, psi, body);
+        if (e == cudaSuccess) h.inv_valid = true;
+        return e;
+    }
+    return run_graph(h, 1, src, psi, [&](cudaStream_t st) { return sweep_dispatch<double, true>(h, a, st); });
 }
+
+bool factor_cache_supported(const Handle& h) { return h.p == 1 && h.dim >= 1 && h.dim <= 3; }
 
 template <int D, int P>
 cudaError_t apply_L_launch(Handle& h, const ApplyArgs& a) {
@@ -25,7 +42,7 @@ cudaError_t apply_L_launch(Handle& h, const ApplyArgs& a) {
 cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y) {
     ApplyArgs a;
     a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
-    a.omega = h.d_omega; a.normals = h.d_normals; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
+    a.omega = h.d_omega; a.dots = h.d_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
     a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
     a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
     a.x = x; a.y = y;
@@ -40,6 +57,7 @@ cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y) {
         case 23: return apply_L_launch<2, 3>(h, a);
         case 30: return apply_L_launch<3, 0>(h, a);
         case 31: return apply_L_launch<3, 1>(h, a);
+        case 32: return apply_L_launch<3, 2>(h, a);
         default: return cudaErrorNotSupported;
     }
 }

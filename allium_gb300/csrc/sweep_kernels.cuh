@@ -13,6 +13,8 @@
 // F(self, nbr) equals F_self with its columns permuted by that map.
 #pragma once
 
+#include <type_traits>
+
 #include "geometry.cuh"
 
 namespace allium {
@@ -24,7 +26,7 @@ struct SweepArgs {
     int ne, Nw, G;
     long long ndof;
     const double* omega;
-    const double* normals;
+    const R* dots;    // [nfaces][Nw] Omega_a . n_f, n_f out of element 1
     const Slot* slots;
     const uint8_t* nbrmap;
     const R* Gm;      // [ne][D][N][N]
@@ -42,6 +44,53 @@ struct SweepArgs {
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
 
+// n contiguous values of one (group, angle, cell) block; 16-byte vectors when
+// the block size allows (the API requires 16-byte aligned vectors)
+template <int N, typename R>
+__device__ __forceinline__ void load_block(const R* p, R (&v)[N]) {
+    if constexpr (sizeof(R) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 4; ++i) {
+            const float4 x = reinterpret_cast<const float4*>(p)[i];
+            v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+        }
+    } else if constexpr (sizeof(R) == 8 && N % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 2; ++i) {
+            const double2 x = reinterpret_cast<const double2*>(p)[i];
+            v[2 * i] = x.x; v[2 * i + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = p[i];
+    }
+}
+
+template <int N, typename R>
+__device__ __forceinline__ void store_block(R* p, const R (&v)[N]) {
+    if constexpr (sizeof(R) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 4; ++i)
+            reinterpret_cast<float4*>(p)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    } else if constexpr (sizeof(R) == 8 && N % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 2; ++i) reinterpret_cast<double2*>(p)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = v[i];
+    }
+}
+
+// Compile-time loop: f(std::integral_constant<int, i>) for i in [B, E).  Keeps
+// every register-array index a constant, so the local system stays in registers.
+template <int B, int E, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
 // Gaussian elimination on registers.  PIVOT: partial pivoting on the largest
 // magnitude (first one on ties), the order mfem::LUFactors::Factor uses.  The
 // right-hand side is eliminated alongside, and back substitution multiplies
@@ -49,149 +98,456 @@ __device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(
 template <int N, bool PIVOT, typename R>
 __device__ __forceinline__ bool solve_local(R (&A)[N][N], R (&b)[N]) {
     bool ok = true;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        if (PIVOT) {
+    static_for<0, N>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        if constexpr (PIVOT) {
             R amax = fabs(A[k][k]);
             int piv = k;
-#pragma unroll
-            for (int i = k + 1; i < N; ++i) {
+            static_for<k + 1, N>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
                 const R v = fabs(A[i][k]);
                 if (v > amax) { amax = v; piv = i; }
-            }
-#pragma unroll
-            for (int i = k + 1; i < N; ++i) {
+            });
+            static_for<k + 1, N>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
                 const bool sw = (piv == i);
-#pragma unroll
-                for (int j = k; j < N; ++j) {
+                static_for<k, N>([&](auto jc) {
+                    constexpr int j = decltype(jc)::value;
                     const R x = A[k][j], y = A[i][j];
                     A[k][j] = sw ? y : x;
                     A[i][j] = sw ? x : y;
-                }
+                });
                 const R x = b[k], y = b[i];
                 b[k] = sw ? y : x;
                 b[i] = sw ? x : y;
-            }
+            });
         }
         const R pk = A[k][k];
         ok = ok && (pk != R(0));
         const R inv = R(1) / pk;
-#pragma unroll
-        for (int i = k + 1; i < N; ++i) {
+        static_for<k + 1, N>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
             const R l = A[i][k] * inv;
-#pragma unroll
-            for (int j = k + 1; j < N; ++j) A[i][j] = fma_r(-l, A[k][j], A[i][j]);
+            static_for<k + 1, N>([&](auto jc) {
+                constexpr int j = decltype(jc)::value;
+                A[i][j] = fma_r(-l, A[k][j], A[i][j]);
+            });
             b[i] = fma_r(-l, b[k], b[i]);
-        }
+        });
         A[k][k] = inv;
-    }
-#pragma unroll
-    for (int k = N - 1; k >= 0; --k) {
+    });
+    static_for<0, N>([&](auto kc) {
+        constexpr int k = N - 1 - decltype(kc)::value;
         const R x = b[k] * A[k][k];
         b[k] = x;
-#pragma unroll
-        for (int i = 0; i < k; ++i) b[i] = fma_r(-A[i][k], x, b[i]);
-    }
+        static_for<0, k>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            b[i] = fma_r(-A[i][k], x, b[i]);
+        });
+    });
     return ok;
 }
 
-template <int D, int P, typename R, bool PIVOT>
-__global__ void __launch_bounds__(128) k_sweep_level(SweepArgs<R> s, const int* __restrict__ nodes, int count) {
-    constexpr int N1 = P + 1;
-    constexpr int N = ipow(N1, D);
-    constexpr int NF = ipow(N1, D - 1);
-    constexpr int NFACE = 2 * D;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)count * s.G) return;
-    const int node = nodes[t / s.G];
-    const int g = (int)(t % s.G);
-    const int e = node / s.Nw;
-    const int a = node - e * s.Nw;
-
-    double om[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-    for (int d = 0; d < D; ++d) om[d] = s.omega[a * D + d];
-
-    R A[N][N];
-    {
-        const R* Gm = s.Gm + (size_t)e * D * N * N;
-        const R* M = s.M + (size_t)e * N * N;
-        const R sg = s.sigma[(size_t)g * s.ne + e];
-#pragma unroll
-        for (int i = 0; i < N; ++i)
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                R v = R(om[0]) * Gm[i * N + j];
-#pragma unroll
-                for (int d = 1; d < D; ++d) v = fma_r(R(om[d]), Gm[d * N * N + i * N + j], v);
-                A[i][j] = fma_r(sg, M[i * N + j], v);
+// In-place inverse by Gauss-Jordan elimination with partial pivoting (row
+// swaps undone as column swaps at the end).
+template <int N>
+__device__ __forceinline__ bool invert_local(double (&A)[N][N]) {
+    bool ok = true;
+    int perm[N];
+    static_for<0, N>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        double amax = fabs(A[k][k]);
+        int piv = k;
+        static_for<k + 1, N>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const double v = fabs(A[i][k]);
+            if (v > amax) { amax = v; piv = i; }
+        });
+        perm[k] = piv;
+        static_for<k + 1, N>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const bool sw = (piv == i);
+            static_for<0, N>([&](auto jc) {
+                constexpr int j = decltype(jc)::value;
+                const double x = A[k][j], y = A[i][j];
+                A[k][j] = sw ? y : x;
+                A[i][j] = sw ? x : y;
+            });
+        });
+        ok = ok && (A[k][k] != 0.0);
+        const double inv = 1.0 / A[k][k];
+        A[k][k] = 1.0;
+        static_for<0, N>([&](auto jc) { A[k][decltype(jc)::value] *= inv; });
+        static_for<0, N>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            if constexpr (i != k) {
+                const double f = A[i][k];
+                A[i][k] = 0.0;
+                static_for<0, N>([&](auto jc) {
+                    constexpr int j = decltype(jc)::value;
+                    A[i][j] = fma(-f, A[k][j], A[i][j]);
+                });
             }
-        if (s.td) {
-            const R* Mt = s.Mt + (size_t)e * N * N;
+        });
+    });
+    static_for<0, N>([&](auto kc) {
+        constexpr int k = N - 1 - decltype(kc)::value;
+        static_for<k + 1, N>([&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            const bool sw = (perm[k] == j);
+            static_for<0, N>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                const double x = A[i][k], y = A[i][j];
+                A[i][k] = sw ? y : x;
+                A[i][j] = sw ? x : y;
+            });
+        });
+    });
+    return ok;
+}
+
+// Local matrix of node (e, a), group g (the assembly part of k_sweep_level).
+template <int D, int P, typename R>
+__device__ __forceinline__ void assemble_local(const SweepArgs<R>& s, int e, int a, int g,
+                                               R (&A)[ipow(P + 1, D)][ipow(P + 1, D)],
+                                               R (&dots)[2 * D], int (&nbrs)[2 * D]) {
+    constexpr int N = ipow(P + 1, D);
+    constexpr int NF = ipow(P + 1, D - 1);
+    constexpr int NFACE = 2 * D;
+    R om[3] = {R(0), R(0), R(0)};
 #pragma unroll
-            for (int i = 0; i < N; ++i)
+    for (int d = 0; d < D; ++d) om[d] = R(s.omega[a * D + d]);
+    const R* Gm = s.Gm + (size_t)e * D * N * N;
+    const R* M = s.M + (size_t)e * N * N;
+    const R sg = s.sigma[(size_t)g * s.ne + e];
+    // whole rows per load: the cell's matrices are shared by the warp's threads
 #pragma unroll
-                for (int j = 0; j < N; ++j) A[i][j] = fma_r(s.tau, Mt[i * N + j], A[i][j]);
+    for (int i = 0; i < N; ++i) {
+        R row[N], mrow[N];
+        load_block<N>(Gm + i * N, row);
+        load_block<N>(M + i * N, mrow);
+#pragma unroll
+        for (int j = 0; j < N; ++j) A[i][j] = om[0] * row[j];
+#pragma unroll
+        for (int d = 1; d < D; ++d) {
+            load_block<N>(Gm + d * N * N + i * N, row);
+#pragma unroll
+            for (int j = 0; j < N; ++j) A[i][j] = fma_r(om[d], row[j], A[i][j]);
+        }
+#pragma unroll
+        for (int j = 0; j < N; ++j) A[i][j] = fma_r(sg, mrow[j], A[i][j]);
+    }
+    if (s.td) {
+        const R* Mt = s.Mt + (size_t)e * N * N;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            R row[N];
+            load_block<N>(Mt + i * N, row);
+#pragma unroll
+            for (int j = 0; j < N; ++j) A[i][j] = fma_r(s.tau, row[j], A[i][j]);
         }
     }
-
-    double dots[NFACE];
-    int nbrs[NFACE];
 #pragma unroll
     for (int k = 0; k < NFACE; ++k) {
         const Slot q = s.slots[(size_t)e * NFACE + k];
-        double nr[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-        for (int d = 0; d < D; ++d) nr[d] = s.normals[(size_t)q.face * D + d];
-        const double d1 = dot_exact(D, om, nr);
-        const double dk = q.side ? -d1 : d1;
+        const R d1 = s.dots[(size_t)q.face * s.Nw + a];
+        const R dk = q.side ? -d1 : d1;
         dots[k] = dk;
         nbrs[k] = q.nbr;
-        if (dk > 0.0) {
+        if (dk > R(0)) {
             const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
-            const R rd = R(dk);
 #pragma unroll
-            for (int ii = 0; ii < NF; ++ii)
+            for (int ii = 0; ii < NF; ++ii) {
+                R frow[NF];
+                load_block<NF>(F + ii * NF, frow);
 #pragma unroll
                 for (int jj = 0; jj < NF; ++jj) {
                     const int fi = face_dof(D, P, k, ii), fj = face_dof(D, P, k, jj);
-                    A[fi][fj] = fma_r(rd, F[ii * NF + jj], A[fi][fj]);
+                    A[fi][fj] = fma_r(dk, frow[jj], A[fi][fj]);
                 }
+            }
         }
     }
+}
 
-    R b[N];
-    {
-        const R* src = s.src + psi_index(s.ndof, s.Nw, g, a, (long long)e * N);
-#pragma unroll
-        for (int i = 0; i < N; ++i) b[i] = src[i];
-    }
+// Right-hand side of node (e, a), group g: q plus the upwind face terms.
+template <int D, int P, typename R>
+__device__ __forceinline__ void assemble_rhs(const SweepArgs<R>& s, int e, int a, int g, const R (&dots)[2 * D],
+                                             const int (&nbrs)[2 * D], R (&b)[ipow(P + 1, D)]) {
+    constexpr int N = ipow(P + 1, D);
+    constexpr int NF = ipow(P + 1, D - 1);
+    constexpr int NFACE = 2 * D;
+    load_block<N>(s.src + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), b);
 #pragma unroll
     for (int k = 0; k < NFACE; ++k) {
-        if (dots[k] < 0.0 && nbrs[k] >= 0) {
+        if (dots[k] < R(0) && nbrs[k] >= 0) {
             const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
             const R* up = s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)nbrs[k] * N);
             R u[NF];
+            if constexpr (NF == 4) {
+                // the four map bytes of a face in one 32-bit load (4-byte aligned: NF = 4)
+                const unsigned m4 = *reinterpret_cast<const unsigned*>(map);
 #pragma unroll
-            for (int jj = 0; jj < NF; ++jj) u[jj] = up[map[jj]];
+                for (int jj = 0; jj < NF; ++jj) u[jj] = up[(m4 >> (8 * jj)) & 0xffu];
+            } else {
+#pragma unroll
+                for (int jj = 0; jj < NF; ++jj) u[jj] = up[map[jj]];
+            }
             const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
-            const R rd = R(-dots[k]);
+            const R rd = -dots[k];
 #pragma unroll
             for (int ii = 0; ii < NF; ++ii) {
+                R frow[NF];
+                load_block<NF>(F + ii * NF, frow);
                 R acc = R(0);
 #pragma unroll
-                for (int jj = 0; jj < NF; ++jj) acc = fma_r(F[ii * NF + jj], u[jj], acc);
+                for (int jj = 0; jj < NF; ++jj) acc = fma_r(frow[jj], u[jj], acc);
                 const int fi = face_dof(D, P, k, ii);
                 b[fi] = fma_r(rd, acc, b[fi]);
             }
         }
     }
+}
 
+template <int D, int P, typename R, bool PIVOT>
+__global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 4 : 1)) k_sweep_level(SweepArgs<R> s, const int* __restrict__ nodes, int count) {
+    constexpr int N = ipow(P + 1, D);
+    // count * G < 2^31 is checked by the launcher
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count * s.G) return;
+    const int ni = t / s.G;
+    const int g = t - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+    R A[N][N], dots[2 * D];
+    int nbrs[2 * D];
+    assemble_local<D, P, R>(s, e, a, g, A, dots, nbrs);
+    R b[N];
+    assemble_rhs<D, P, R>(s, e, a, g, dots, nbrs, b);
     if (!solve_local<N, PIVOT>(A, b)) atomicOr(s.status, kErrSingular);
+    store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), b);
+}
 
-    R* out = s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N);
+
+// ---------------------------------------------------------------- team kernel
+// One team of T lanes (T = smallest power of two >= N, N <= 32) per (cell,
+// angle, group) node; lane r owns row r of the local system.  Rows of the cell
+// matrices and of q/psi are read by consecutive lanes (coalesced), elimination
+// runs on warp shuffles inside the team, so a lane holds one row (~N + 10
+// registers) instead of the whole matrix.  PIVOT: partial pivoting by a team
+// argmax (largest magnitude, lowest row on ties) and a row exchange between
+// the two lanes.
+__host__ __device__ constexpr int team_size(int n) {
+    return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32;
+}
+
+template <int D, int P, typename R, bool PIVOT>
+__global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* __restrict__ nodes, int count) {
+    constexpr int N1 = P + 1;
+    constexpr int N = ipow(N1, D);
+    constexpr int NF = ipow(N1, D - 1);
+    constexpr int NFACE = 2 * D;
+    constexpr int T = team_size(N);
+    static_assert(N <= 32, "team kernel handles local systems up to 32 x 32");
+    const int lane = threadIdx.x & 31;
+    const int r = lane & (T - 1);
+    const unsigned mask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
+    const int team = (blockIdx.x * blockDim.x + threadIdx.x) / T;
+    if (team >= count * s.G) return;   // whole teams leave together
+    const bool act = r < N;
+    const int ni = team / s.G;
+    const int g = team - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+
+    // this lane's row: tensor indices of local DOF r
+    int rid[3] = {0, 0, 0};
+    {
+        int q = r;
 #pragma unroll
-    for (int i = 0; i < N; ++i) out[i] = b[i];
+        for (int d = 0; d < D; ++d) { rid[d] = q % N1; q /= N1; }
+    }
+
+    R Ar[N];
+    R br = R(0);
+    {
+        R om[3] = {R(0), R(0), R(0)};
+#pragma unroll
+        for (int d = 0; d < D; ++d) om[d] = R(s.omega[a * D + d]);
+        const int rr = act ? r : 0;
+        const R* Gm = s.Gm + (size_t)e * D * N * N + rr * N;
+        const R* M = s.M + (size_t)e * N * N + rr * N;
+        const R sg = s.sigma[(size_t)g * s.ne + e];
+        R row[N];
+        load_block<N>(Gm, row);
+#pragma unroll
+        for (int j = 0; j < N; ++j) Ar[j] = om[0] * row[j];
+#pragma unroll
+        for (int d = 1; d < D; ++d) {
+            load_block<N>(Gm + d * N * N, row);
+#pragma unroll
+            for (int j = 0; j < N; ++j) Ar[j] = fma_r(om[d], row[j], Ar[j]);
+        }
+        load_block<N>(M, row);
+#pragma unroll
+        for (int j = 0; j < N; ++j) Ar[j] = fma_r(sg, row[j], Ar[j]);
+        if (s.td) {
+            load_block<N>(s.Mt + (size_t)e * N * N + rr * N, row);
+#pragma unroll
+            for (int j = 0; j < N; ++j) Ar[j] = fma_r(s.tau, row[j], Ar[j]);
+        }
+        if (act) br = s.src[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)];
+    }
+
+    static_for<0, NFACE>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int ax = k / 2, side = k % 2;
+        const Slot q = s.slots[(size_t)e * NFACE + k];
+        const R d1 = s.dots[(size_t)q.face * s.Nw + a];
+        const R dk = q.side ? -d1 : d1;
+        // is row r on face k, and which face DOF is it
+        const bool on = act && (rid[ax] == side * P);
+        int ii = 0, stride = 1;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            if (d != ax) { ii += rid[d] * stride; stride *= N1; }
+        const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF + ii * NF;
+        if (dk > R(0) && on) {
+            R frow[NF];
+            load_block<NF>(F, frow);
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) {
+                const int fj = face_dof(D, P, k, jj);
+                Ar[fj] = fma_r(dk, frow[jj], Ar[fj]);
+            }
+        }
+        if (dk < R(0) && q.nbr >= 0 && on) {
+            const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
+            const R* up = s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)q.nbr * N);
+            R frow[NF];
+            load_block<NF>(F, frow);
+            R acc = R(0);
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) acc = fma_r(frow[jj], up[map[jj]], acc);
+            br = fma_r(-dk, acc, br);
+        }
+    });
+
+    bool ok = true;
+    static_for<0, N>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        if constexpr (PIVOT) {
+            // team argmax of |A[i][k]| over rows i >= k
+            R best = (r >= k && act) ? fabs(Ar[k]) : R(-1);
+            int bi = r;
+#pragma unroll
+            for (int off = T / 2; off > 0; off >>= 1) {
+                const R ob = __shfl_xor_sync(mask, best, off, T);
+                const int oi = __shfl_xor_sync(mask, bi, off, T);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            const int p = bi;   // same on every lane of the team
+            const int src = (r == k) ? p : (r == p ? k : r);
+#pragma unroll
+            for (int j = k; j < N; ++j) Ar[j] = __shfl_sync(mask, Ar[j], src, T);
+            br = __shfl_sync(mask, br, src, T);
+        }
+        const R akk = __shfl_sync(mask, Ar[k], k, T);
+        ok = ok && (akk != R(0));
+        const R inv = R(1) / akk;
+        const R l = Ar[k] * inv;
+        const R bk = __shfl_sync(mask, br, k, T);
+#pragma unroll
+        for (int j = k + 1; j < N; ++j) {
+            const R akj = __shfl_sync(mask, Ar[j], k, T);
+            if (r > k) Ar[j] = fma_r(-l, akj, Ar[j]);
+        }
+        if (r > k) br = fma_r(-l, bk, br);
+        if (r == k) Ar[k] = inv;
+    });
+    static_for<0, N>([&](auto kc) {
+        constexpr int k = N - 1 - decltype(kc)::value;
+        const R xk = __shfl_sync(mask, br * Ar[k], k, T);
+        if (r == k) br = xk;
+        if (r < k) br = fma_r(-Ar[k], xk, br);
+    });
+    if (!ok && r == 0) atomicOr(s.status, kErrSingular);
+    if (act) s.psi[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)] = br;
+}
+
+// FP64 sweep that also keeps the inverse of every local matrix.  The inverse
+// of node-group t of the level-sorted order is stored entry-major,
+// inv[(i*N + j) * stride + t], so a warp's loads of one entry are contiguous.
+template <int D, int P>
+__global__ void __launch_bounds__(128) k_sweep_factor_level(SweepArgs<double> s, const int* __restrict__ nodes,
+                                                            int count, double* __restrict__ inv,
+                                                            long long stride, long long base) {
+    constexpr int N = ipow(P + 1, D);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count * s.G) return;
+    const int ni = t / s.G;
+    const int g = t - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+    double A[N][N], dots[2 * D];
+    int nbrs[2 * D];
+    assemble_local<D, P, double>(s, e, a, g, A, dots, nbrs);
+    double b[N];
+    assemble_rhs<D, P, double>(s, e, a, g, dots, nbrs, b);
+    if (!invert_local<N>(A)) atomicOr(s.status, kErrSingular);
+    double x[N];
+    double* out = inv + base + t;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        double acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            out[(size_t)(i * N + j) * stride] = A[i][j];
+            acc = fma(A[i][j], b[j], acc);
+        }
+        x[i] = acc;
+    }
+    store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), x);
+}
+
+// FP64 sweep with the stored inverses: psi = inv(A) (q + upwind terms).
+template <int D, int P>
+__global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<double> s, const int* __restrict__ nodes,
+                                                            int count, const double* __restrict__ inv,
+                                                            long long stride, long long base) {
+    constexpr int N = ipow(P + 1, D);
+    constexpr int NFACE = 2 * D;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count * s.G) return;
+    const int ni = t / s.G;
+    const int g = t - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+    double dots[NFACE];
+    int nbrs[NFACE];
+#pragma unroll
+    for (int k = 0; k < NFACE; ++k) {
+        const Slot q = s.slots[(size_t)e * NFACE + k];
+        const double d1 = s.dots[(size_t)q.face * s.Nw + a];
+        dots[k] = q.side ? -d1 : d1;
+        nbrs[k] = q.nbr;
+    }
+    double b[N];
+    assemble_rhs<D, P, double>(s, e, a, g, dots, nbrs, b);
+    const double* in = inv + base + t;
+    double x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        double acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < N; ++j) acc = fma(__ldg(in + (size_t)(i * N + j) * stride), b[j], acc);
+        x[i] = acc;
+    }
+    store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), x);
 }
 
 // y = L x (AdvectionOperator::Mult, src/sweep.cpp:1246-1387) from the cell's
@@ -202,7 +558,7 @@ struct ApplyArgs {
     int ne, Nw, G;
     long long ndof;
     const double* omega;
-    const double* normals;
+    const double* dots;
     const Slot* slots;
     const uint8_t* nbrmap;
     const double *Gm, *M, *Mt, *F, *sigma;
@@ -256,10 +612,7 @@ __global__ void __launch_bounds__(128) k_apply_L(ApplyArgs s) {
 #pragma unroll
     for (int k = 0; k < NFACE; ++k) {
         const Slot q = s.slots[(size_t)e * NFACE + k];
-        double nr[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-        for (int d = 0; d < D; ++d) nr[d] = s.normals[(size_t)q.face * D + d];
-        const double d1 = dot_exact(D, om, nr);
+        const double d1 = s.dots[(size_t)q.face * s.Nw + a];
         const double dk = q.side ? -d1 : d1;
         const double* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
         if (dk > 0.0) {

@@ -6,32 +6,74 @@
 namespace allium {
 
 template <int D, int P, typename R, bool PIVOT>
-cudaError_t sweep_levels(Handle& h, const SweepArgs<R>& args) {
+cudaError_t sweep_levels(Handle& h, const SweepArgs<R>& args, cudaStream_t stream) {
     constexpr int kBlock = 128;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = h.h_level_offsets[l];
         const int count = h.h_level_offsets[l + 1] - off;
         if (count == 0) continue;
         const long long threads = (long long)count * h.G;
+        if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_level<D, P, R, PIVOT><<<grid, kBlock, 0, h.stream>>>(args, h.d_level_nodes + off, count);
+        k_sweep_level<D, P, R, PIVOT><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count);
     }
     return cudaGetLastError();
 }
 
+template <int D, int P, typename R, bool PIVOT>
+cudaError_t sweep_levels_team(Handle& h, const SweepArgs<R>& args, cudaStream_t stream) {
+    constexpr int kBlock = 256;
+    constexpr int T = team_size(ipow(P + 1, D));
+    for (int l = 0; l < h.num_levels; ++l) {
+        const int off = h.h_level_offsets[l];
+        const int count = h.h_level_offsets[l + 1] - off;
+        if (count == 0) continue;
+        const long long threads = (long long)count * h.G * T;
+        if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
+        const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
+        k_sweep_team<D, P, R, PIVOT><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count);
+    }
+    return cudaGetLastError();
+}
+
+// mode 0: plain; 1: plain + store inverses; 2: from stored inverses (FP64)
+template <int D, int P>
+cudaError_t sweep_levels_inv(Handle& h, const SweepArgs<double>& args, int mode, cudaStream_t stream) {
+    constexpr int kBlock = 128;
+    const long long stride = (long long)h.G * h.ne * h.Nw;
+    for (int l = 0; l < h.num_levels; ++l) {
+        const int off = h.h_level_offsets[l];
+        const int count = h.h_level_offsets[l + 1] - off;
+        if (count == 0) continue;
+        const long long threads = (long long)count * h.G;
+        if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
+        const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
+        const long long base = (long long)off * h.G;
+        if (mode == 1)
+            k_sweep_factor_level<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, h.d_inv, stride, base);
+        else
+            k_sweep_cached_level<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, h.d_inv, stride, base);
+    }
+    return cudaGetLastError();
+}
+
+// Thread per node while the local system fits a thread's registers (N <= 8):
+// fewest instructions per node, and every lane busy on the FP64 pipe.  Team
+// kernel (lane per row) for the larger systems, which would spill.
 template <typename R, bool PIVOT>
-cudaError_t sweep_dispatch(Handle& h, const SweepArgs<R>& a) {
+cudaError_t sweep_dispatch(Handle& h, const SweepArgs<R>& a, cudaStream_t st) {
     switch (h.dim * 10 + h.p) {
-        case 10: return sweep_levels<1, 0, R, PIVOT>(h, a);
-        case 11: return sweep_levels<1, 1, R, PIVOT>(h, a);
-        case 12: return sweep_levels<1, 2, R, PIVOT>(h, a);
-        case 13: return sweep_levels<1, 3, R, PIVOT>(h, a);
-        case 20: return sweep_levels<2, 0, R, PIVOT>(h, a);
-        case 21: return sweep_levels<2, 1, R, PIVOT>(h, a);
-        case 22: return sweep_levels<2, 2, R, PIVOT>(h, a);
-        case 23: return sweep_levels<2, 3, R, PIVOT>(h, a);
-        case 30: return sweep_levels<3, 0, R, PIVOT>(h, a);
-        case 31: return sweep_levels<3, 1, R, PIVOT>(h, a);
+        case 10: return sweep_levels<1, 0, R, PIVOT>(h, a, st);
+        case 11: return sweep_levels<1, 1, R, PIVOT>(h, a, st);
+        case 12: return sweep_levels<1, 2, R, PIVOT>(h, a, st);
+        case 13: return sweep_levels<1, 3, R, PIVOT>(h, a, st);
+        case 20: return sweep_levels<2, 0, R, PIVOT>(h, a, st);
+        case 21: return sweep_levels<2, 1, R, PIVOT>(h, a, st);
+        case 22: return sweep_levels_team<2, 2, R, PIVOT>(h, a, st);
+        case 23: return sweep_levels_team<2, 3, R, PIVOT>(h, a, st);
+        case 30: return sweep_levels<3, 0, R, PIVOT>(h, a, st);
+        case 31: return sweep_levels<3, 1, R, PIVOT>(h, a, st);
+        case 32: return sweep_levels_team<3, 2, R, PIVOT>(h, a, st);
         default: return cudaErrorNotSupported;
     }
 }

@@ -123,6 +123,10 @@ class InverseAdvectionOperator:
         check(_lib.lib().allium_sweep_mult_f32(self.h, C.c_void_p(_ptr(source, np.float32, self.width, "source")),
                                                C.c_void_p(_ptr(psi, np.float32, self.height, "psi"))), self.h)
 
+    def SetFactorCache(self, mode):
+        """1: keep FP64 local-matrix inverses across Mults when memory allows (default); 0: off."""
+        check(_lib.lib().allium_sweep_set_factor_cache(self.h, int(mode)), self.h)
+
     def AssembleLocalMatrices(self, sigma_t=None):
         if sigma_t is None:
             sigma_t = self._keep[6]

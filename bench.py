@@ -8,7 +8,11 @@ boundaries, q uniform in [0, 1] per cell.  A step is one InverseAdvectionOperato
 Mult (one full sweep of every cell, angle and group).  The metric is swept
 cell-angle-group DOF per second = G * Nw * Ndof / sweep time.
 
-  value     FP64 sweep with q and psi resident in HBM (CUDA events)
+  value     FP64 sweep with q and psi resident in HBM (CUDA events), in the
+            library's default mode: the first Mult after (re)assembly stores
+            the inverse of every local system, later Mults apply them (two
+            different sources alternate over the timed steps); the uncached
+            FP64 sweep and the first Mult are reported beside it
   e2e       the same Mult through the C ABI with pinned host buffers, the
             host->device copy of q and the device->host copy of psi inside the
             timed region (wall clock around the synchronous call)
@@ -180,6 +184,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed(stream, steps, fn):
+    """Average ms per call of fn(i) over `steps` calls, CUDA events on `stream`."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        fn(i)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def run_gpu(args):
     import torch
     from allium_gb300.sweep import FormTransportSource, InverseAdvectionOperator
@@ -195,68 +211,72 @@ def run_gpu(args):
 
     cells = (args.cells,) * 3
     mesh, quad, sigma, q = workload(cells)
-    L = InverseAdvectionOperator(mesh, ORDER, quad, sigma)
+    L = InverseAdvectionOperator(mesh, ORDER, quad, sigma)   # runs on torch's current stream
     stream = torch.cuda.current_stream()
     N = L.width
     src_host = FormTransportSource(L, q)
-    src = torch.from_numpy(src_host).cuda()
-    psi = torch.empty_like(src)
+    # two different sources, alternated over the timed steps
+    srcs = [torch.from_numpy(src_host).cuda(), torch.from_numpy(src_host[::-1].copy()).cuda()]
+    psi = torch.empty_like(srcs[0])
 
     def barrier():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
 
-    # --- FP64, resident in HBM
-    for _ in range(args.warmup):
-        L.Mult(src, psi)
-    L.synchronize()
-    barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clk = ClockSampler(local).__enter__()   # sampled across all timed regions below
-    ev0.record(stream)
-    for _ in range(args.steps):
-        L.Mult(src, psi)
-    ev1.record(stream)
-    L.synchronize()
-    barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        return float(t.item())
+
+    clk = ClockSampler(local).__enter__()   # sampled across all timed regions below
+
+    # --- FP64 without the factor cache (every Mult refactors, as the reference does)
+    L.SetFactorCache(0)
+    for i in range(args.warmup):
+        L.Mult(srcs[i % 2], psi)
+    barrier()
+    ms_plain = max_over_ranks(_timed(stream, max(3, args.steps // 10), lambda i: L.Mult(srcs[i % 2], psi)))
+
+    # --- FP64 with the factor cache: the first Mult factors, later ones reuse
+    L.SetFactorCache(1)
+    barrier()
+    ms_first = max_over_ranks(_timed(stream, 1, lambda i: L.Mult(srcs[0], psi)))
+    for i in range(args.warmup):
+        L.Mult(srcs[i % 2], psi)
+    barrier()
+    ms = max_over_ranks(_timed(stream, args.steps, lambda i: L.Mult(srcs[i % 2], psi)))
+    barrier()
     value = world * N / (ms * 1e-3)
+    L.Mult(srcs[0], psi)
+    L.synchronize()
 
     # --- FP32 sweep, resident
-    f_src = src.float()
+    f_src = srcs[0].float()
     f_psi = torch.empty_like(f_src)
     for _ in range(args.warmup):
         L.MultF32(f_src, f_psi)
     L.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        L.MultF32(f_src, f_psi)
-    ev1.record(stream)
-    L.synchronize()
-    ms32 = ev0.elapsed_time(ev1) / args.steps
+    ms32 = _timed(stream, args.steps, lambda i: L.MultF32(f_src, f_psi))
     err32 = float((torch.max(torch.abs(f_psi.double() - psi)) / torch.max(torch.abs(psi))).item())
     del f_src, f_psi
 
-    # --- e2e through the C ABI with pinned host buffers
-    h_src = torch.from_numpy(src_host).pin_memory()
-    h_psi = torch.empty_like(h_src).pin_memory()
-    L.Mult(h_src, h_psi)
+    # --- e2e through the C ABI with pinned host buffers (copies inside the timed region)
+    h_srcs = [s.cpu().pin_memory() for s in srcs]
+    h_psi = torch.empty_like(h_srcs[0]).pin_memory()
+    L.Mult(h_srcs[0], h_psi)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        L.Mult(h_src, h_psi)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    for i in range(args.steps):
+        L.Mult(h_srcs[i % 2], h_psi)
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     e2e = world * N / e2e_s
     clk.__exit__(None, None, None)
+    L.Mult(h_srcs[(args.steps - 1) % 2], h_psi)
+    L.Mult(srcs[(args.steps - 1) % 2], psi)
+    L.synchronize()
     assert torch.equal(h_psi, psi.cpu()), "host and device paths disagree"
 
     if rank != 0:
@@ -264,17 +284,15 @@ def run_gpu(args):
             dist.destroy_process_group()
         return
 
-    # roofline of the dominant kernel (the FP64 sweep kernel, all level launches of one Mult)
     peak, peak_kind = measured_peaks()
     alg_bytes = 16.0 * N + 8.0 * mesh.num_elements * (1 + 3 * 8)
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     tpe = traffic_per_entry()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": (tpe * N if tpe is not None else None), "peak_kind": peak_kind,
-            "kernel": "k_sweep_level<3,1,double,pivot>", "algorithmic_bytes_per_launch": alg_bytes,
-            "launch": "one Mult = all wavefront-level launches of the sweep kernel"}
-    # FP64 compute roofline for context: ~147 FP64 FMA per swept entry
-    fp64_flops = 2 * 590.0 * N / 8
+            "kernel": "k_sweep_cached_level<3,1> (FP64 sweep from stored local inverses)",
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "launch": "one Mult = the CUDA graph of all wavefront-level launches"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(L.num_levels, cells),
@@ -282,7 +300,10 @@ def run_gpu(args):
                     "ms_per_step": e2e_s * 1e3},
             "gpu_launches": args.steps * L.num_levels,
             "roofline": roof,
-            "fp64_compute": {"achieved_tflops": fp64_flops / (ms * 1e-3) / 1e12, "nominal_peak_tflops": 1.25},
+            "fp64_uncached": {"value": N / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                              "note": "every Mult assembles and factors all local systems (pivoted LU), as the reference does"},
+            "fp64_first_mult_ms": ms_first,
+            "factor_cache_bytes": N * 8 * 8,
             "fp32": {"value": N / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32,
                      "max_rel_err_vs_fp64": err32,
                      "roofline_frac": (8.0 * N / (ms32 * 1e-3) / 1e9) / peak},

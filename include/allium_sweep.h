@@ -68,7 +68,7 @@ typedef struct {
     const int* boundary_attributes;     /* [num_boundary_faces] */
 } allium_mesh_desc;
 
-/* L2 DG space: order p in 0..3, Gauss-Lobatto basis, lumping bit mask
+/* L2 DG space: order p in 0..3 (0..2 on hexahedra), Gauss-Lobatto basis, lumping bit mask
  * (allium's `lump` constructor argument, src/sweep.hpp:83). */
 typedef struct {
     int order;
@@ -106,7 +106,9 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe,
 /* ~InverseAdvectionOperator (src/sweep.cpp:246-257). */
 void allium_sweep_destroy(allium_sweep* s);
 
-/* Use the given cudaStream_t (NULL = the handle's own stream). */
+/* Enqueue all further work of the handle on the given cudaStream_t; NULL
+ * selects the CUDA default stream.  Until this is called the handle uses a
+ * non-blocking stream of its own. */
 int allium_sweep_set_stream(allium_sweep* s, void* cuda_stream);
 
 /* Width()/Height() of the operator (src/sweep.cpp:29): psi_size = G*Nw*Ndof. */
@@ -125,6 +127,15 @@ int allium_sweep_set_time_absorption(allium_sweep* s, double tau);
  * partially pivoted local LU.  source may equal psi (in-place Mult(psi, psi),
  * as transport_op.hpp:28 and chive.cpp:733 call it). */
 int allium_sweep_mult(allium_sweep* s, const double* source, double* psi);
+
+/* FP64 factor cache (no counterpart in the reference, which refactors every
+ * local system on every Mult).  mode 1 (default): on the first FP64 Mult after
+ * construction, AssembleLocalMatrices or a new time absorption, the sweep also
+ * stores the inverse of every (cell, angle, group) local matrix (G*Nw*Ne*n*n
+ * doubles, 22.5 GB for 64^3 cells, p = 1, S12) when that needs at most half of
+ * the free device memory; later Mults apply the stored inverses instead of
+ * factoring.  mode 0: never cache (frees the cache). */
+int allium_sweep_set_factor_cache(allium_sweep* s, int mode);
 
 /* The same sweep with FP32 storage and FP32 local solves (unpivoted
  * elimination; the local upwind matrix has a positive definite symmetric part

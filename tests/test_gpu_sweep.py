@@ -39,6 +39,8 @@ CASES = [
     (3, (5, 4, 3), 1, 4, 2, 0.0, 0),
     (3, (6, 6, 6), 1, 12, 1, 0.1, 0),
     (3, (4, 4, 4), 1, 4, 1, 0.0, 7),
+    (3, (4, 3, 3), 2, 4, 1, 0.0, 0),
+    (3, (4, 4, 4), 2, 6, 2, 0.1, 0),
 ]
 
 
@@ -84,6 +86,35 @@ def test_sweep_parity(case):
     # balance
     b = AdvectionOperator(L).ComputeBalance(ref)
     assert abs(b - o.balance(ref)) < TOL64 * abs(o.balance(ref))
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c[2] == 1], ids=[f"d{c[0]}S{c[3]}G{c[4]}l{c[6]}" for c in CASES if c[2] == 1])
+def test_factor_cache(case):
+    # the FP64 factor cache (stored local inverses) against the plain sweep and
+    # the oracle; repeated Mults replay the same captured launches bit for bit
+    mesh, quad, sig, o, L = build(*case)
+    src = np.random.default_rng(8).random(o.psi_size)
+    L.SetFactorCache(0)
+    plain = np.empty_like(src)
+    L.Mult(src, plain)
+    L.SetFactorCache(1)
+    d_src = torch.from_numpy(src).cuda()
+    out = torch.empty_like(d_src)
+    L.Mult(d_src, out)          # factors and stores the inverses
+    first = out.cpu().numpy()
+    L.Mult(d_src, out)          # applies the stored inverses
+    second = out.cpu().numpy()
+    L.Mult(d_src, out)
+    L.synchronize()
+    assert np.array_equal(first, second) and np.array_equal(second, out.cpu().numpy())
+    assert rel_err(first, plain) < TOL64
+    assert rel_err(first, o.mult(src)) < TOL64
+    # new cross sections invalidate the stored inverses
+    sig2 = sig * 2.0 + 0.3
+    L.AssembleLocalMatrices(sig2)
+    L.Mult(d_src, out)
+    L.synchronize()
+    assert rel_err(out.cpu().numpy(), OracleSweep(mesh, case[2], quad, sig2, lump=case[6]).mult(src)) < TOL64
 
 
 @pytest.mark.parametrize("case", CASES[:: 2], ids=[f"d{c[0]}p{c[2]}" for c in CASES[:: 2]])
@@ -139,7 +170,8 @@ def test_time_absorption(dim, cells):
     assert rel_err(psi, o2.mult(src)) < TOL64
 
 
-@pytest.mark.parametrize("dim,cells,p", [(1, (10,), 3), (2, (10, 10), 2), (3, (6, 6, 6), 1), (3, (10, 10, 10), 0)])
+@pytest.mark.parametrize("dim,cells,p", [(1, (10,), 3), (2, (10, 10), 2), (2, (10, 10), 3), (3, (6, 6, 6), 1),
+                                         (3, (10, 10, 10), 0), (3, (3, 3, 3), 2)])
 def test_constant_solution(dim, cells, p):
     # test_sweep.cpp:7-108 on the GPU: sigma = 0, q = 0, unit inflow -> psi == 1
     mesh = M.cartesian(cells)
@@ -251,9 +283,9 @@ def test_errors_are_reported():
     with pytest.raises(AlliumError) as e:
         InverseAdvectionOperator(mesh, 1, quad, sig, bc={1: "reflective"})
     assert e.value.status == 7
-    m3, q3, s3 = problem(3, (2, 2, 2), 2)
+    m3, q3, s3 = problem(3, (2, 2, 2), 3)
     with pytest.raises(AlliumError) as e:
-        InverseAdvectionOperator(m3, 2, q3, s3)
+        InverseAdvectionOperator(m3, 3, q3, s3)
     assert e.value.status == 7
     L = InverseAdvectionOperator(mesh, 1, quad, sig)
     x = np.zeros(L.width)
