@@ -48,6 +48,7 @@ EXPORTS = {
     "allium_sweep_mult_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_apply_L": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_balance_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_moments": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "allium_sweep_moments_transpose": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "allium_sweep_form_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
