@@ -53,6 +53,8 @@ EXPORTS = {
     "allium_sweep_moments_transpose": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "allium_sweep_form_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "allium_sweep_scattering_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_moments_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_scattering_source_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_levels": (C.c_int, [C.c_void_p, C.c_void_p]),
     "allium_sweep_synchronize": (C.c_int, [C.c_void_p]),
     "allium_sweep_last_error": (C.c_char_p, [C.c_void_p]),

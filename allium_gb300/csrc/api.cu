@@ -62,7 +62,8 @@ void free_all(Handle& h) {
     if (h.capture_stream) cudaStreamDestroy(h.capture_stream);
     void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
-                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv};
+                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv, h.f_inv,
+                    h.d_sigma_s};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -248,25 +249,28 @@ int allium_sweep_scattering_source(allium_sweep* s, const double* sigma_s, const
     Handle& h = s->h;
     int st = ensure_mass2(h);
     if (st) return st;
+    st = upload(h, sigma_s, (size_t)h.G * h.ne, &h.d_sigma_s);
+    if (st) return st;
     const size_t pbytes = (size_t)h.psi_size * sizeof(double);
     const size_t mbytes = (size_t)h.G * h.ndof * sizeof(double);
-    double *dsig = nullptr, *dphi = nullptr, *dq = nullptr;
-    st = upload(h, sigma_s, (size_t)h.G * h.ne, &dsig);
-    const bool dph = on_device(phi), dqf = q_fixed && on_device(q_fixed), dout = on_device(out);
+    const bool dph = on_device(phi), dqf = !q_fixed || on_device(q_fixed), dout = on_device(out);
+    if (dph && dqf && dout) {
+        CUDA_OR_FAIL(h, allium::launch_scatter_source(h, h.d_sigma_s, phi, q_fixed, out));
+        return ALLIUM_OK;
+    }
+    double *dphi = nullptr, *dq = nullptr;
     cudaError_t e = cudaSuccess;
     const double* xp = phi;
     const double* xq = q_fixed;
     double* y = out;
-    if (!st && !dph) { e = cudaMalloc(&dphi, mbytes); if (e == cudaSuccess) e = cudaMemcpyAsync(dphi, phi, mbytes, cudaMemcpyHostToDevice, h.stream); xp = dphi; }
-    if (!st && e == cudaSuccess && q_fixed && !dqf) { e = cudaMalloc(&dq, pbytes); if (e == cudaSuccess) e = cudaMemcpyAsync(dq, q_fixed, pbytes, cudaMemcpyHostToDevice, h.stream); xq = dq; }
-    if (!st && e == cudaSuccess && !dout) { e = ensure(&h.d_stage, (size_t)h.psi_size); y = h.d_stage; }
-    if (!st && e == cudaSuccess) e = allium::launch_scatter_source(h, dsig, xp, xq, y);
-    if (!st && e == cudaSuccess && !dout) e = cudaMemcpyAsync(out, y, pbytes, cudaMemcpyDeviceToHost, h.stream);
-    if (!st && e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
-    if (dsig) cudaFree(dsig);
+    if (!dph) { e = cudaMalloc(&dphi, mbytes); if (e == cudaSuccess) e = cudaMemcpyAsync(dphi, phi, mbytes, cudaMemcpyHostToDevice, h.stream); xp = dphi; }
+    if (e == cudaSuccess && !dqf) { e = cudaMalloc(&dq, pbytes); if (e == cudaSuccess) e = cudaMemcpyAsync(dq, q_fixed, pbytes, cudaMemcpyHostToDevice, h.stream); xq = dq; }
+    if (e == cudaSuccess && !dout) { e = ensure(&h.d_stage, (size_t)h.psi_size); y = h.d_stage; }
+    if (e == cudaSuccess) e = allium::launch_scatter_source(h, h.d_sigma_s, xp, xq, y);
+    if (e == cudaSuccess && !dout) e = cudaMemcpyAsync(out, y, pbytes, cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
     if (dphi) cudaFree(dphi);
     if (dq) cudaFree(dq);
-    if (st) return st;
     CUDA_OR_FAIL(h, e);
     return ALLIUM_OK;
 }
@@ -277,20 +281,28 @@ static bool misaligned(const void* a, const void* b, bool da, bool db) {
 
 // Allocate the FP64 factor cache when enabled, supported and it leaves at
 // least half of the free device memory untouched; otherwise sweep without it.
-static void prepare_factor_cache(Handle& h) {
-    if (h.d_inv || h.factor_cache == 0 || !allium::factor_cache_supported(h)) return;
-    const size_t need = (size_t)h.G * h.ne * h.Nw * h.n * h.n * sizeof(double);
+static void prepare_factor_cache(Handle& h, bool fp32) {
+    if (h.factor_cache == 0 || !allium::factor_cache_supported(h)) return;
+    if (h.d_inv && (!fp32 || h.f_inv)) return;
+    const size_t entries = (size_t)h.G * h.ne * h.Nw * h.n * h.n;
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return; }
+    const size_t need = (h.d_inv ? 0 : entries * sizeof(double)) + (fp32 && !h.f_inv ? entries * sizeof(float) : 0);
     if (need > free_b / 2) return;
-    if (cudaMalloc(&h.d_inv, need) != cudaSuccess) { cudaGetLastError(); h.d_inv = nullptr; return; }
-    h.inv_valid = false;
+    if (!h.d_inv && cudaMalloc(&h.d_inv, entries * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError(); h.d_inv = nullptr; return;
+    }
+    if (fp32 && !h.f_inv && cudaMalloc(&h.f_inv, entries * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError(); h.f_inv = nullptr; return;
+    }
+    h.inv_valid = false;   // (re)factor so the new buffer is filled
+    allium::drop_graphs(h);
 }
 
 int allium_sweep_mult(allium_sweep* s, const double* source, double* psi) {
     if (!s || !source || !psi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
-    prepare_factor_cache(h);
+    prepare_factor_cache(h, false);
     const bool ds = on_device(source), dp = on_device(psi);
     if (misaligned(source, psi, ds, dp)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
     if (ds && dp) {
@@ -314,6 +326,7 @@ int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi) {
     if (!s || !source || !psi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
     if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
+    prepare_factor_cache(h, true);
     const bool ds = on_device(source), dp = on_device(psi);
     if (misaligned(source, psi, ds, dp)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
     if (ds && dp) {
@@ -428,6 +441,30 @@ int allium_sweep_moments_transpose(allium_sweep* s, const double* phi, double* p
     return ALLIUM_OK;
 }
 
+int allium_sweep_moments_f32(allium_sweep* s, const float* psi, double* phi) {
+    if (!s || !psi || !phi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!on_device(psi) || !on_device(phi)) { h.last_error = "allium_sweep_moments_f32 takes device vectors"; return ALLIUM_ERR_ARG; }
+    CUDA_OR_FAIL(h, allium::launch_moments_f32(h, psi, phi));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_scattering_source_f32(allium_sweep* s, const double* sigma_s, const double* phi,
+                                       const float* q_fixed, float* out) {
+    if (!s || !sigma_s || !phi || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!on_device(phi) || !on_device(out) || (q_fixed && !on_device(q_fixed))) {
+        h.last_error = "allium_sweep_scattering_source_f32 takes device vectors";
+        return ALLIUM_ERR_ARG;
+    }
+    int st = ensure_mass2(h);
+    if (st) return st;
+    st = upload(h, sigma_s, (size_t)h.G * h.ne, &h.d_sigma_s);
+    if (st) return st;
+    CUDA_OR_FAIL(h, allium::launch_scatter_source_f32(h, h.d_sigma_s, phi, q_fixed, out));
+    return ALLIUM_OK;
+}
+
 int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow, int num_attr, double* source) {
     if (!s || !source || (inflow && num_attr < 1)) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
@@ -469,7 +506,9 @@ int allium_sweep_set_factor_cache(allium_sweep* s, int mode) {
         CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
         allium::drop_graphs(h);
         cudaFree(h.d_inv);
+        if (h.f_inv) cudaFree(h.f_inv);
         h.d_inv = nullptr;
+        h.f_inv = nullptr;
         h.inv_valid = false;
     }
     return ALLIUM_OK;

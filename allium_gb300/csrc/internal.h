@@ -65,11 +65,13 @@ struct Handle {
     float* f_stage = nullptr;
     double* d_scratch = nullptr;     // reduction partials
     size_t scratch_len = 0;
+    double* d_sigma_s = nullptr;     // last scattering cross sections uploaded [G][Ne]
     bool fp32_ready = false;
     // FP64 factor cache: inverse of every local matrix, entry-major over the
     // level-sorted node-group order (allocated on the first FP64 Mult when it fits)
     int factor_cache = 1;            // 0 off, 1 automatic
     double* d_inv = nullptr;
+    float* f_inv = nullptr;          // FP32 copy, for the FP32 sweep
     bool inv_valid = false;
 
     // CUDA graphs of the per-level launch sequence, keyed by kind and vectors
@@ -151,6 +153,8 @@ cudaError_t launch_moments_transpose(Handle& h, const double* phi, double* psi, 
 cudaError_t launch_balance(Handle& h, const double* psi, double* partial, int nblocks_max, int* nblocks);
 cudaError_t launch_balance_finish(Handle& h, const double* partial, int nparts, double* out);
 cudaError_t launch_scatter_source(Handle& h, const double* sigma_s, const double* phi, const double* qfix, double* out);
+cudaError_t launch_moments_f32(Handle& h, const float* psi, double* phi);
+cudaError_t launch_scatter_source_f32(Handle& h, const double* sigma_s, const double* phi, const float* qfix, float* out);
 cudaError_t make_fp32_copies(Handle& h);
 RefTables make_ref_tables(int dim, int p, int lump);
 
@@ -159,6 +163,7 @@ cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi);
 cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi);
 cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y);
 bool factor_cache_supported(const Handle& h);
+cudaError_t ensure_factors(Handle& h);
 
 }  // namespace allium
 

@@ -689,6 +689,53 @@ cudaError_t launch_scatter_source(Handle& h, const double* sigma_s, const double
     return cudaGetLastError();
 }
 
+// FP32 psi -> FP64 moments (zeroth moment, FP64 accumulation over angles)
+__global__ void k_moments_f32(int Nw, int G, long long ndof, const double* __restrict__ w,
+                              const float* __restrict__ psi, double* __restrict__ phi) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    double acc = 0.0;
+    for (int a = 0; a < Nw; ++a) acc = fma(w[a], (double)psi[psi_index(ndof, Nw, g, a, s)], acc);
+    phi[s + ndof * g] = acc;
+}
+
+cudaError_t launch_moments_f32(Handle& h, const float* psi, double* phi) {
+    const long long total = (long long)h.G * h.ndof;
+    const int b = 256;
+    k_moments_f32<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.Nw, h.G, h.ndof, h.d_weights, psi, phi);
+    return cudaGetLastError();
+}
+
+// FP32 scattering source: out = (float)(D^T (S phi) + q_fixed), S phi in FP64
+__global__ void k_scatter_source_f32(int ne, int Nw, int G, int n, long long ndof, double wsum,
+                                     const double* __restrict__ Ms, const double* __restrict__ sigma_s,
+                                     const double* __restrict__ phi, const float* qfix, float* out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    const int e = (int)(s / n), i = (int)(s % n);
+    const double* M = Ms + (size_t)e * n * n + (size_t)i * n;
+    const double* ph = phi + ndof * g + (long long)e * n;
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) acc += M[j] * ph[j];
+    const double v = (sigma_s[(size_t)g * ne + e] * acc) / wsum;
+    for (int a = 0; a < Nw; ++a) {
+        const long long k = psi_index(ndof, Nw, g, a, s);
+        out[k] = qfix ? (float)((double)qfix[k] + v) : (float)v;
+    }
+}
+
+cudaError_t launch_scatter_source_f32(Handle& h, const double* sigma_s, const double* phi, const float* qfix, float* out) {
+    const long long total = (long long)h.G * h.ndof;
+    const int b = 256;
+    k_scatter_source_f32<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.ne, h.Nw, h.G, h.n, h.ndof, h.wsum, h.d_Mt,
+                                                                              sigma_s, phi, qfix, out);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ FP32 copies
 __global__ void k_to_f32(const double* __restrict__ in, float* __restrict__ out, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

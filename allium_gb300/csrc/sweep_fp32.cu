@@ -10,6 +10,11 @@ cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi) {
     a.Gm = h.f_G; a.M = h.f_M; a.Mt = h.f_Mt; a.F = h.f_F; a.sigma = h.f_sigma;
     a.tau = (float)h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status;
+    if (h.f_inv) {
+        cudaError_t e = ensure_factors(h);
+        if (e != cudaSuccess) return e;
+        return run_graph(h, 4, src, psi, [&](cudaStream_t st) { return cached_dispatch<float>(h, a, h.f_inv, st); });
+    }
     return run_graph(h, 3, src, psi, [&](cudaStream_t st) { return sweep_dispatch<float, false>(h, a, st); });
 }
 

@@ -3,6 +3,27 @@
 
 namespace allium {
 
+// (Re)compute the stored inverses when they are stale: FP64, and the FP32
+// copy when that buffer exists.
+cudaError_t ensure_factors(Handle& h) {
+    if (h.inv_valid) return cudaSuccess;
+    SweepArgs<double> a;
+    a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
+    a.omega = h.d_omega; a.dots = h.d_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
+    a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
+    a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
+    a.src = nullptr; a.psi = nullptr; a.status = h.d_status;
+    cudaError_t e;
+    switch (h.dim * 10 + h.p) {
+        case 11: e = factor_all<1, 1>(h, a); break;
+        case 21: e = factor_all<2, 1>(h, a); break;
+        case 31: e = factor_all<3, 1>(h, a); break;
+        default: e = cudaErrorNotSupported;
+    }
+    if (e == cudaSuccess) h.inv_valid = true;
+    return e;
+}
+
 cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
     SweepArgs<double> a;
     a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
@@ -11,19 +32,9 @@ cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
     a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status;
     if (h.d_inv) {
-        const int mode = h.inv_valid ? 2 : 1;
-        auto body = [&](cudaStream_t st) -> cudaError_t {
-            switch (h.dim * 10 + h.p) {
-                case 11: return sweep_levels_inv<1, 1>(h, a, mode, st);
-                case 21: return sweep_levels_inv<2, 1>(h, a, mode, st);
-                case 31: return sweep_levels_inv<3, 1>(h, a, mode, st);
-                default: return cudaErrorNotSupported;
-            }
-        };
-        // the factor pass runs once per operator: launch it directly
-        cudaError_t e = (mode == 1) ? body(h.stream) : run_graph(h, 2, src, psi, body);
-        if (e == cudaSuccess) h.inv_valid = true;
-        return e;
+        cudaError_t e = ensure_factors(h);
+        if (e != cudaSuccess) return e;
+        return run_graph(h, 2, src, psi, [&](cudaStream_t st) { return cached_dispatch<double>(h, a, h.d_inv, st); });
     }
     return run_graph(h, 1, src, psi, [&](cudaStream_t st) { return sweep_dispatch<double, true>(h, a, st); });
 }

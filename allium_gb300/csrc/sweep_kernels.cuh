@@ -477,46 +477,41 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
     if (act) s.psi[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)] = br;
 }
 
-// FP64 sweep that also keeps the inverse of every local matrix.  The inverse
-// of node-group t of the level-sorted order is stored entry-major,
-// inv[(i*N + j) * stride + t], so a warp's loads of one entry are contiguous.
+// Inverse of every local matrix, in one pass over all node-groups of all levels
+// (no level ordering needed: the local matrices do not depend on upstream
+// data).  Node-group t of the level-sorted order is stored entry-major,
+// inv[(i*N + j) * stride + t], so a warp's loads of one entry are contiguous;
+// inv32 (optional) receives the same inverse rounded to FP32.
 template <int D, int P>
-__global__ void __launch_bounds__(128) k_sweep_factor_level(SweepArgs<double> s, const int* __restrict__ nodes,
-                                                            int count, double* __restrict__ inv,
-                                                            long long stride, long long base) {
+__global__ void __launch_bounds__(128) k_factor_all(SweepArgs<double> s, const int* __restrict__ nodes,
+                                                    long long total, double* __restrict__ inv64,
+                                                    float* __restrict__ inv32) {
     constexpr int N = ipow(P + 1, D);
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count * s.G) return;
-    const int ni = t / s.G;
-    const int g = t - ni * s.G;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const long long ni = t / s.G;
+    const int g = (int)(t - ni * s.G);
     const int node = nodes[ni];
     const int e = node / s.Nw;
     const int a = node - e * s.Nw;
     double A[N][N], dots[2 * D];
     int nbrs[2 * D];
     assemble_local<D, P, double>(s, e, a, g, A, dots, nbrs);
-    double b[N];
-    assemble_rhs<D, P, double>(s, e, a, g, dots, nbrs, b);
     if (!invert_local<N>(A)) atomicOr(s.status, kErrSingular);
-    double x[N];
-    double* out = inv + base + t;
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-        double acc = 0.0;
+    for (int i = 0; i < N; ++i)
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            out[(size_t)(i * N + j) * stride] = A[i][j];
-            acc = fma(A[i][j], b[j], acc);
+            const size_t k = (size_t)(i * N + j) * total + t;
+            if (inv64) inv64[k] = A[i][j];
+            if (inv32) inv32[k] = (float)A[i][j];
         }
-        x[i] = acc;
-    }
-    store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), x);
 }
 
-// FP64 sweep with the stored inverses: psi = inv(A) (q + upwind terms).
-template <int D, int P>
-__global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<double> s, const int* __restrict__ nodes,
-                                                            int count, const double* __restrict__ inv,
+// Sweep with the stored inverses: psi = inv(A) (q + upwind terms).
+template <int D, int P, typename R>
+__global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, const int* __restrict__ nodes,
+                                                            int count, const R* __restrict__ inv,
                                                             long long stride, long long base) {
     constexpr int N = ipow(P + 1, D);
     constexpr int NFACE = 2 * D;
@@ -527,24 +522,24 @@ __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<double> s,
     const int node = nodes[ni];
     const int e = node / s.Nw;
     const int a = node - e * s.Nw;
-    double dots[NFACE];
+    R dots[NFACE];
     int nbrs[NFACE];
 #pragma unroll
     for (int k = 0; k < NFACE; ++k) {
         const Slot q = s.slots[(size_t)e * NFACE + k];
-        const double d1 = s.dots[(size_t)q.face * s.Nw + a];
+        const R d1 = s.dots[(size_t)q.face * s.Nw + a];
         dots[k] = q.side ? -d1 : d1;
         nbrs[k] = q.nbr;
     }
-    double b[N];
-    assemble_rhs<D, P, double>(s, e, a, g, dots, nbrs, b);
-    const double* in = inv + base + t;
-    double x[N];
+    R b[N];
+    assemble_rhs<D, P, R>(s, e, a, g, dots, nbrs, b);
+    const R* in = inv + base + t;
+    R x[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-        double acc = 0.0;
+        R acc = R(0);
 #pragma unroll
-        for (int j = 0; j < N; ++j) acc = fma(__ldg(in + (size_t)(i * N + j) * stride), b[j], acc);
+        for (int j = 0; j < N; ++j) acc = fma_r(__ldg(in + (size_t)(i * N + j) * stride), b[j], acc);
         x[i] = acc;
     }
     store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), x);

@@ -36,9 +36,18 @@ cudaError_t sweep_levels_team(Handle& h, const SweepArgs<R>& args, cudaStream_t 
     return cudaGetLastError();
 }
 
-// mode 0: plain; 1: plain + store inverses; 2: from stored inverses (FP64)
+// All-node factor pass and the sweep from stored inverses (p = 1).
 template <int D, int P>
-cudaError_t sweep_levels_inv(Handle& h, const SweepArgs<double>& args, int mode, cudaStream_t stream) {
+cudaError_t factor_all(Handle& h, const SweepArgs<double>& args) {
+    constexpr int kBlock = 128;
+    const long long total = (long long)h.G * h.ne * h.Nw;
+    const unsigned grid = (unsigned)((total + kBlock - 1) / kBlock);
+    k_factor_all<D, P><<<grid, kBlock, 0, h.stream>>>(args, h.d_level_nodes, total, h.d_inv, h.f_inv);
+    return cudaGetLastError();
+}
+
+template <int D, int P, typename R>
+cudaError_t sweep_levels_cached(Handle& h, const SweepArgs<R>& args, const R* inv, cudaStream_t stream) {
     constexpr int kBlock = 128;
     const long long stride = (long long)h.G * h.ne * h.Nw;
     for (int l = 0; l < h.num_levels; ++l) {
@@ -48,13 +57,20 @@ cudaError_t sweep_levels_inv(Handle& h, const SweepArgs<double>& args, int mode,
         const long long threads = (long long)count * h.G;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        const long long base = (long long)off * h.G;
-        if (mode == 1)
-            k_sweep_factor_level<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, h.d_inv, stride, base);
-        else
-            k_sweep_cached_level<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, h.d_inv, stride, base);
+        k_sweep_cached_level<D, P, R><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, inv, stride,
+                                                                   (long long)off * h.G);
     }
     return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t cached_dispatch(Handle& h, const SweepArgs<R>& a, const R* inv, cudaStream_t st) {
+    switch (h.dim * 10 + h.p) {
+        case 11: return sweep_levels_cached<1, 1, R>(h, a, inv, st);
+        case 21: return sweep_levels_cached<2, 1, R>(h, a, inv, st);
+        case 31: return sweep_levels_cached<3, 1, R>(h, a, inv, st);
+        default: return cudaErrorNotSupported;
+    }
 }
 
 // Thread per node while the local system fits a thread's registers (N <= 8):

@@ -229,6 +229,23 @@ def ScatteringSource(Linv: InverseAdvectionOperator, sigma_s, phi, q_fixed=None,
     return out
 
 
+def ScatteringSourceF32(Linv: InverseAdvectionOperator, sigma_s, phi, q_fixed, out):
+    """FP32 out = D^T (S phi) + q_fixed (S phi in FP64); device tensors only."""
+    sig = np.ascontiguousarray(sigma_s, dtype=np.float64).reshape(Linv.G, -1)
+    qp = _ptr(q_fixed, np.float32, Linv.width, "q_fixed") if q_fixed is not None else None
+    check(_lib.lib().allium_sweep_scattering_source_f32(
+        Linv.h, C.c_void_p(sig.ctypes.data), C.c_void_p(_ptr(phi, np.float64, Linv.G * Linv.ndof, "phi")),
+        C.c_void_p(qp), C.c_void_p(_ptr(out, np.float32, Linv.width, "out"))), Linv.h)
+    return out
+
+
+def MomentsF32(Linv: InverseAdvectionOperator, psi, phi):
+    """FP64 zeroth moment of an FP32 psi; device tensors only."""
+    check(_lib.lib().allium_sweep_moments_f32(Linv.h, C.c_void_p(_ptr(psi, np.float32, Linv.width, "psi")),
+                                              C.c_void_p(_ptr(phi, np.float64, Linv.G * Linv.ndof, "phi"))), Linv.h)
+    return phi
+
+
 def FormTransportSource(Linv: InverseAdvectionOperator, q_cell=None, inflow=None, out=None):
     """Weak-form source for an isotropic density q_cell[G, Ne] and an isotropic
     inflow[G, num_attr] indexed by boundary attribute (vacuum where 0)."""

@@ -167,6 +167,77 @@ def cpu_sweep_sample(threads, steps, warmup):
     return rates, o.psi_size
 
 
+def solve_section(L, mesh, quad, sigma, src, maxiter=400):
+    """Time to a 1e-8 relative residual of T phi = b on the 3D workload with
+    sigma_s / sigma_t ~ U[0.5, 0.999] per cell: FP64 GMRES(30) with the FP64
+    sweep against FP32-inner / FP64-outer refinement (both without DSA)."""
+    import torch
+    from allium_gb300.solvers import SchurOperator, refine, solve_gmres, true_residual
+    rng = np.random.default_rng(SEED + 2)
+    sigma_s = sigma * rng.uniform(0.5, 0.999, size=sigma.shape)
+    # operator setup shared by both: stored FP64 and FP32 local inverses
+    f = src.float()
+    L.MultF32(f, f)
+    torch.cuda.synchronize()
+    del f
+    out = {}
+    op = SchurOperator(L, sigma_s)
+    plain = solve_gmres(op, src, tol=1e-8, restart=30, maxiter=maxiter)
+    b = op.rhs(src)
+    out["fp64_gmres"] = {"seconds": plain.seconds, "iterations": plain.iterations, "converged": plain.converged,
+                         "fp64_sweeps": plain.sweeps64, "residual": true_residual(op, b, plain.phi)}
+    op2 = SchurOperator(L, sigma_s)
+    ir = refine(op2, src, tol=1e-8, inner_tol=1e-4, restart=30)
+    out["fp32_inner_fp64_outer"] = {"seconds": ir.seconds, "outer": ir.iterations,
+                                    "inner_iterations": getattr(ir, "inner_iterations", None),
+                                    "converged": ir.converged, "fp64_sweeps": ir.sweeps64, "fp32_sweeps": ir.sweeps32,
+                                    "residual": true_residual(op2, b, ir.phi)}
+    out["speedup"] = plain.seconds / ir.seconds if ir.seconds > 0 else None
+    out["phi_rel_diff"] = float((torch.max(torch.abs(ir.phi - plain.phi)) / torch.max(torch.abs(plain.phi))).item())
+    out["problem"] = "3D workload, sigma_s/sigma_t ~ U[0.5,0.999] per cell, tol 1e-8 on ||b - T phi||/||b||, no DSA"
+    return out
+
+
+def chive2d_section(cpu=True):
+    """The 2D chive configuration: 64x64 quads, p = 1, S8, sigma_t = 1,
+    sigma_s = 0.9, q = 1, vacuum; source iteration to 1e-8 relative change of
+    phi on the GPU (FP64 sweep), and the CPU oracle doing the same iteration."""
+    import torch
+    from allium_gb300 import mesh as M
+    from allium_gb300 import quadrature as Q
+    from allium_gb300.solvers import SchurOperator, source_iteration
+    from allium_gb300.sweep import FormTransportSource, InverseAdvectionOperator
+    mesh = M.cartesian((64, 64))
+    quad = Q.level_symmetric(8, 2)
+    ne = mesh.num_elements
+    sig_t, sig_s, q = np.ones((1, ne)), np.full((1, ne), 0.9), np.ones((1, ne))
+    L = InverseAdvectionOperator(mesh, 1, quad, sig_t)
+    src = torch.from_numpy(FormTransportSource(L, q)).cuda()
+    source_iteration(SchurOperator(L, sig_s), src, tol=1e-8)   # warm-up (graphs, factors)
+    res = source_iteration(SchurOperator(L, sig_s), src, tol=1e-8)
+    out = {"gpu_si": {"seconds": res.seconds, "iterations": res.iterations, "converged": res.converged}}
+    if cpu:
+        from oracle.oracle import OracleSweep
+        o = OracleSweep(mesh, 1, quad, sig_t)
+        src_h = o.form_source(q_cell=q)
+        t0 = time.perf_counter()
+        phi = np.zeros(o.ndof)
+        it = 0
+        for it in range(1, 5001):
+            psi = o.scattering_source(sig_s, phi, src_h)
+            o.mult(psi, psi, threads=os.cpu_count() or 1)
+            new = o.moments(psi)
+            change = np.linalg.norm(new - phi) / np.linalg.norm(new)
+            phi = new
+            if change < 1e-8:
+                break
+        cpu_s = time.perf_counter() - t0
+        out["cpu_si"] = {"seconds": cpu_s, "iterations": it, "cores": os.cpu_count(), "kind": "port"}
+        out["phi_rel_diff_gpu_vs_cpu"] = float(np.max(np.abs(res.phi.cpu().numpy() - phi)) / np.max(np.abs(phi)))
+        out["speedup_vs_cpu"] = cpu_s / res.seconds
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -308,6 +379,9 @@ def run_gpu(args):
                      "max_rel_err_vs_fp64": err32,
                      "roofline_frac": (8.0 * N / (ms32 * 1e-3) / 1e9) / peak},
             "clocks": clk.summary()}
+    if not args.no_solve:
+        line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0])
+        line["chive_2d"] = chive2d_section(cpu=not args.no_cpu)
     if not args.no_cpu and tuple(cells) == CELLS:
         rates, size = cpu_sweep_sample(os.cpu_count() or 1, 3, 1)
         line["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": os.cpu_count(),
@@ -326,6 +400,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cells", type=int, default=CELLS[0], help="cells per axis (smaller cases for profiling)")
+    ap.add_argument("--no-solve", action="store_true", help="skip the time-to-tolerance solves")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

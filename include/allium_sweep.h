@@ -187,6 +187,14 @@ int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double
 int allium_sweep_scattering_source(allium_sweep* s, const double* sigma_s, const double* phi,
                                    const double* q_fixed, double* out);
 
+/* FP32 companions for the inner iterations of an FP64 outer solve (device
+ * vectors only): zeroth moment of an FP32 psi accumulated in FP64, and the
+ * scattering source D^T (S phi) + q_fixed computed in FP64 and stored in FP32
+ * (q_fixed FP32 or NULL). */
+int allium_sweep_moments_f32(allium_sweep* s, const float* psi, double* phi);
+int allium_sweep_scattering_source_f32(allium_sweep* s, const double* sigma_s, const double* phi,
+                                       const float* q_fixed, float* out);
+
 /* Wavefront level of every (cell, angle) node e*Nw + a (the Kahn frontier
  * index of src/sweep.cpp:308-512), host or device int array [Ne*Nw]. */
 int allium_sweep_levels(allium_sweep* s, int* levels);
