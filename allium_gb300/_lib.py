@@ -45,6 +45,7 @@ EXPORTS = {
     "allium_sweep_set_time_absorption": (C.c_int, [C.c_void_p, C.c_double]),
     "allium_sweep_mult": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_set_factor_cache": (C.c_int, [C.c_void_p, C.c_int]),
+    "allium_sweep_set_schedule": (C.c_int, [C.c_void_p, C.c_int]),
     "allium_sweep_mult_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_apply_L": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -55,7 +56,13 @@ EXPORTS = {
     "allium_sweep_scattering_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_moments_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_scattering_source_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_to_node_layout_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_from_node_layout_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_mult_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_scattering_source_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_moments_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_levels": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "allium_sweep_selftest_wait": (C.c_int, [C.c_void_p, C.c_int]),
     "allium_sweep_synchronize": (C.c_int, [C.c_void_p]),
     "allium_sweep_last_error": (C.c_char_p, [C.c_void_p]),
     "allium_status_string": (C.c_char_p, [C.c_int]),

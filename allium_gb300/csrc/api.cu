@@ -1,5 +1,6 @@
 // C ABI of liballium_sweep.so (declared in include/allium_sweep.h).
 #include <cstdint>
+#include <initializer_list>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -51,6 +52,7 @@ int check_status(Handle& h) {
     if (st) {
         CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_status, 0, sizeof(int), h.stream));
         if (st & allium::kErrSingular) { h.last_error = "zero pivot in a local solve"; return ALLIUM_ERR_SINGULAR; }
+        if (st & allium::kErrTimeout) { h.last_error = "a bounded device wait gave up"; return ALLIUM_ERR_TIMEOUT; }
         h.last_error = "non-finite value";
         return ALLIUM_ERR_NAN;
     }
@@ -62,8 +64,8 @@ void free_all(Handle& h) {
     if (h.capture_stream) cudaStreamDestroy(h.capture_stream);
     void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
-                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv, h.f_inv,
-                    h.d_sigma_s};
+                    h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
+                    h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -281,28 +283,23 @@ static bool misaligned(const void* a, const void* b, bool da, bool db) {
 
 // Allocate the FP64 factor cache when enabled, supported and it leaves at
 // least half of the free device memory untouched; otherwise sweep without it.
-static void prepare_factor_cache(Handle& h, bool fp32) {
-    if (h.factor_cache == 0 || !allium::factor_cache_supported(h)) return;
-    if (h.d_inv && (!fp32 || h.f_inv)) return;
-    const size_t entries = (size_t)h.G * h.ne * h.Nw * h.n * h.n;
+// Allocate the FP64 factor cache when enabled, supported and it leaves at
+// least half of the free device memory untouched; otherwise sweep without it.
+static void prepare_factor_cache(Handle& h) {
+    if (h.d_inv || h.factor_cache == 0 || !allium::factor_cache_supported(h)) return;
+    const size_t need = (size_t)h.G * h.ne * h.Nw * h.n * h.n * sizeof(double);
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return; }
-    const size_t need = (h.d_inv ? 0 : entries * sizeof(double)) + (fp32 && !h.f_inv ? entries * sizeof(float) : 0);
     if (need > free_b / 2) return;
-    if (!h.d_inv && cudaMalloc(&h.d_inv, entries * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError(); h.d_inv = nullptr; return;
-    }
-    if (fp32 && !h.f_inv && cudaMalloc(&h.f_inv, entries * sizeof(float)) != cudaSuccess) {
-        cudaGetLastError(); h.f_inv = nullptr; return;
-    }
-    h.inv_valid = false;   // (re)factor so the new buffer is filled
+    if (cudaMalloc(&h.d_inv, need) != cudaSuccess) { cudaGetLastError(); h.d_inv = nullptr; return; }
+    h.inv_valid = false;
     allium::drop_graphs(h);
 }
 
 int allium_sweep_mult(allium_sweep* s, const double* source, double* psi) {
     if (!s || !source || !psi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
-    prepare_factor_cache(h, false);
+    prepare_factor_cache(h);
     const bool ds = on_device(source), dp = on_device(psi);
     if (misaligned(source, psi, ds, dp)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
     if (ds && dp) {
@@ -326,7 +323,6 @@ int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi) {
     if (!s || !source || !psi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
     if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
-    prepare_factor_cache(h, true);
     const bool ds = on_device(source), dp = on_device(psi);
     if (misaligned(source, psi, ds, dp)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
     if (ds && dp) {
@@ -465,6 +461,59 @@ int allium_sweep_scattering_source_f32(allium_sweep* s, const double* sigma_s, c
     return ALLIUM_OK;
 }
 
+static int device_only(Handle& h, std::initializer_list<const void*> ptrs, const char* who) {
+    for (const void* p : ptrs)
+        if (p && !on_device(p)) { h.last_error = std::string(who) + " takes device vectors"; return ALLIUM_ERR_ARG; }
+    return ALLIUM_OK;
+}
+
+int allium_sweep_to_node_layout_f32(allium_sweep* s, const double* psi, float* out) {
+    if (!s || !psi || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {psi, out}, "allium_sweep_to_node_layout_f32")) return st;
+    CUDA_OR_FAIL(h, allium::launch_layout(h, 1, psi, out));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_from_node_layout_f32(allium_sweep* s, const float* in, double* psi) {
+    if (!s || !in || !psi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {in, psi}, "allium_sweep_from_node_layout_f32")) return st;
+    CUDA_OR_FAIL(h, allium::launch_layout(h, 0, in, psi));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_mult_f32_nodes(allium_sweep* s, const float* source, float* psi) {
+    if (!s || !source || !psi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {source, psi}, "allium_sweep_mult_f32_nodes")) return st;
+    if (misaligned(source, psi, true, true)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
+    if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
+    CUDA_OR_FAIL(h, allium::launch_sweep_nodes_f32(h, source, psi));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_scattering_source_f32_nodes(allium_sweep* s, const double* sigma_s, const double* phi,
+                                             const float* q_nodes, float* out) {
+    if (!s || !sigma_s || !phi || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {phi, q_nodes, out}, "allium_sweep_scattering_source_f32_nodes")) return st;
+    int st = ensure_mass2(h);
+    if (st) return st;
+    st = upload(h, sigma_s, (size_t)h.G * h.ne, &h.d_sigma_s);
+    if (st) return st;
+    CUDA_OR_FAIL(h, allium::launch_scatter_nodes(h, h.d_sigma_s, phi, q_nodes, out));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_moments_f32_nodes(allium_sweep* s, const float* psi, double* phi) {
+    if (!s || !psi || !phi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {psi, phi}, "allium_sweep_moments_f32_nodes")) return st;
+    CUDA_OR_FAIL(h, allium::launch_moments_nodes(h, psi, phi));
+    return ALLIUM_OK;
+}
+
 int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow, int num_attr, double* source) {
     if (!s || !source || (inflow && num_attr < 1)) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
@@ -506,12 +555,28 @@ int allium_sweep_set_factor_cache(allium_sweep* s, int mode) {
         CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
         allium::drop_graphs(h);
         cudaFree(h.d_inv);
-        if (h.f_inv) cudaFree(h.f_inv);
         h.d_inv = nullptr;
-        h.f_inv = nullptr;
         h.inv_valid = false;
     }
     return ALLIUM_OK;
+}
+
+int allium_sweep_set_schedule(allium_sweep* s, int mode) {
+    if (!s || mode < 0 || mode > 1) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (mode != h.schedule) {
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+        allium::drop_graphs(h);
+        h.schedule = mode;
+    }
+    return ALLIUM_OK;
+}
+
+int allium_sweep_selftest_wait(allium_sweep* s, int poll_limit) {
+    if (!s || poll_limit < 1 || poll_limit > (1 << 20)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    CUDA_OR_FAIL(h, allium::launch_wait_probe(h, poll_limit));
+    return check_status(h);
 }
 
 int allium_sweep_synchronize(allium_sweep* s) {

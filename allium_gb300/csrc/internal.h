@@ -71,7 +71,6 @@ struct Handle {
     // level-sorted node-group order (allocated on the first FP64 Mult when it fits)
     int factor_cache = 1;            // 0 off, 1 automatic
     double* d_inv = nullptr;
-    float* f_inv = nullptr;          // FP32 copy, for the FP32 sweep
     bool inv_valid = false;
 
     // CUDA graphs of the per-level launch sequence, keyed by kind and vectors
@@ -86,6 +85,14 @@ struct Handle {
     int graph_next = 0;
     cudaStream_t capture_stream = nullptr;
     bool use_graphs = true;
+
+    // dataflow schedule (one persistent launch per sweep)
+    int schedule = 0;                // 0: one launch per wavefront level, 1: dataflow
+    unsigned* d_flags = nullptr;     // [ne * Nw * G]
+    unsigned* d_flow_words = nullptr;   // [0] epoch, [1] tile counter
+    int* d_tile_start = nullptr;
+    int* d_tile_count = nullptr;
+    int ntiles = 0;
 
     std::string last_error;
 };
@@ -130,6 +137,9 @@ inline void drop_graphs(Handle& h) {
 // kernel error bits (d_status)
 constexpr int kErrSingular = 1;
 constexpr int kErrNaN = 2;
+constexpr int kErrTimeout = 4;
+// node-groups per tile of the dataflow schedule (= threads per block)
+constexpr int kTile = 128;
 
 // ---- topology (topology.cpp, host)
 struct Topology {
@@ -162,6 +172,12 @@ RefTables make_ref_tables(int dim, int p, int lump);
 cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi);
 cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi);
 cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y);
+cudaError_t launch_sweep_nodes_f32(Handle& h, const float* src, float* psi);
+cudaError_t prepare_flow(Handle& h);
+cudaError_t launch_wait_probe(Handle& h, int limit);
+cudaError_t launch_layout(Handle& h, int to_nodes, const void* in, void* out);
+cudaError_t launch_scatter_nodes(Handle& h, const double* sigma_s, const double* phi, const float* qn, float* out);
+cudaError_t launch_moments_nodes(Handle& h, const float* psi, double* phi);
 bool factor_cache_supported(const Handle& h);
 cudaError_t ensure_factors(Handle& h);
 

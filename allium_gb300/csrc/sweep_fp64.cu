@@ -1,7 +1,44 @@
 // FP64 sweep (partially pivoted local LU) and the FP64 forward operator.
+#include <vector>
+
 #include "sweep_launch.cuh"
 
 namespace allium {
+
+// Tile table (tiles never span two levels), completion flags and the
+// epoch/counter words of the dataflow schedule.
+cudaError_t prepare_flow(Handle& h) {
+    if (h.d_flags) return cudaSuccess;
+    std::vector<int> start, count;
+    for (int l = 0; l < h.num_levels; ++l) {
+        const long long first = (long long)h.h_level_offsets[l] * h.G;
+        const long long ng = (long long)(h.h_level_offsets[l + 1] - h.h_level_offsets[l]) * h.G;
+        for (long long k = 0; k < ng; k += kTile) {
+            start.push_back((int)(first + k));
+            count.push_back((int)(ng - k < kTile ? ng - k : kTile));
+        }
+    }
+    h.ntiles = (int)start.size();
+    const size_t nflags = (size_t)h.ne * h.Nw * h.G;
+    cudaError_t e;
+    if ((e = cudaMalloc(&h.d_tile_start, start.size() * sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.d_tile_count, count.size() * sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.d_flow_words, 2 * sizeof(unsigned))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.d_flags, nflags * sizeof(unsigned))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(h.d_tile_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice, h.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(h.d_tile_count, count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice, h.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(h.d_flow_words, 0, 2 * sizeof(unsigned), h.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(h.d_flags, 0, nflags * sizeof(unsigned), h.stream)) != cudaSuccess) return e;
+    return cudaStreamSynchronize(h.stream);   // host vectors go out of scope
+}
+
+cudaError_t launch_wait_probe(Handle& h, int limit) {
+    cudaError_t e = prepare_flow(h);
+    if (e != cudaSuccess) return e;
+    // flags of this handle never hold the value ~0u: the wait can only give up
+    k_wait_probe<<<1, 1, 0, h.stream>>>(h.d_flags, ~0u, limit, h.d_status);
+    return cudaGetLastError();
+}
 
 // (Re)compute the stored inverses when they are stale: FP64, and the FP32
 // copy when that buffer exists.
@@ -31,11 +68,20 @@ cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
     a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
     a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status;
+    const bool flow = h.schedule == 1 && h.p <= 1;
+    if (flow) {
+        cudaError_t e = prepare_flow(h);
+        if (e != cudaSuccess) return e;
+    }
     if (h.d_inv) {
         cudaError_t e = ensure_factors(h);
         if (e != cudaSuccess) return e;
+        if (flow)
+            return run_graph(h, 12, src, psi, [&](cudaStream_t st) { return flow_dispatch<0, double>(h, a, h.d_inv, st); });
         return run_graph(h, 2, src, psi, [&](cudaStream_t st) { return cached_dispatch<double>(h, a, h.d_inv, st); });
     }
+    if (flow)
+        return run_graph(h, 11, src, psi, [&](cudaStream_t st) { return flow_dispatch<1, double>(h, a, nullptr, st); });
     return run_graph(h, 1, src, psi, [&](cudaStream_t st) { return sweep_dispatch<double, true>(h, a, st); });
 }
 

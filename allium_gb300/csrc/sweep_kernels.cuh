@@ -271,7 +271,12 @@ __device__ __forceinline__ void assemble_local(const SweepArgs<R>& s, int e, int
 }
 
 // Right-hand side of node (e, a), group g: q plus the upwind face terms.
-template <int D, int P, typename R>
+template <typename R>
+__device__ __forceinline__ R load_upstream(const R* p, bool cg) {
+    return cg ? __ldcg(p) : *p;
+}
+
+template <int D, int P, typename R, bool CG = false>
 __device__ __forceinline__ void assemble_rhs(const SweepArgs<R>& s, int e, int a, int g, const R (&dots)[2 * D],
                                              const int (&nbrs)[2 * D], R (&b)[ipow(P + 1, D)]) {
     constexpr int N = ipow(P + 1, D);
@@ -288,10 +293,10 @@ __device__ __forceinline__ void assemble_rhs(const SweepArgs<R>& s, int e, int a
                 // the four map bytes of a face in one 32-bit load (4-byte aligned: NF = 4)
                 const unsigned m4 = *reinterpret_cast<const unsigned*>(map);
 #pragma unroll
-                for (int jj = 0; jj < NF; ++jj) u[jj] = up[(m4 >> (8 * jj)) & 0xffu];
+                for (int jj = 0; jj < NF; ++jj) u[jj] = load_upstream(up + ((m4 >> (8 * jj)) & 0xffu), CG);
             } else {
 #pragma unroll
-                for (int jj = 0; jj < NF; ++jj) u[jj] = up[map[jj]];
+                for (int jj = 0; jj < NF; ++jj) u[jj] = load_upstream(up + map[jj], CG);
             }
             const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
             const R rd = -dots[k];
@@ -480,12 +485,10 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
 // Inverse of every local matrix, in one pass over all node-groups of all levels
 // (no level ordering needed: the local matrices do not depend on upstream
 // data).  Node-group t of the level-sorted order is stored entry-major,
-// inv[(i*N + j) * stride + t], so a warp's loads of one entry are contiguous;
-// inv32 (optional) receives the same inverse rounded to FP32.
+// inv[(i*N + j) * stride + t], so a warp's loads of one entry are contiguous.
 template <int D, int P>
 __global__ void __launch_bounds__(128) k_factor_all(SweepArgs<double> s, const int* __restrict__ nodes,
-                                                    long long total, double* __restrict__ inv64,
-                                                    float* __restrict__ inv32) {
+                                                    long long total, double* __restrict__ inv64) {
     constexpr int N = ipow(P + 1, D);
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total) return;
@@ -501,11 +504,7 @@ __global__ void __launch_bounds__(128) k_factor_all(SweepArgs<double> s, const i
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
-        for (int j = 0; j < N; ++j) {
-            const size_t k = (size_t)(i * N + j) * total + t;
-            if (inv64) inv64[k] = A[i][j];
-            if (inv32) inv32[k] = (float)A[i][j];
-        }
+        for (int j = 0; j < N; ++j) inv64[(size_t)(i * N + j) * total + t] = A[i][j];
 }
 
 // Sweep with the stored inverses: psi = inv(A) (q + upwind terms).
@@ -543,6 +542,321 @@ __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, cons
         x[i] = acc;
     }
     store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), x);
+}
+
+
+// ------------------------------------------------------------ node-major FP32 sweep
+// Internal layout for the inner iterations of the FP64 outer solve:
+//   v[((e * Nw + a) * G + g) * N + i]
+// (cell, angle, group, DOF).  In a wavefront level the threads of a warp hold
+// consecutive angles of one cell, so their q/psi blocks and their upwind traces
+// (same octant, same upwind neighbour) are contiguous runs.
+__host__ __device__ inline long long node_index(int Nw, int G, int N, int e, int a, int g) {
+    return (((long long)e * Nw + a) * G + g) * N;
+}
+
+template <int D, int P>
+__global__ void __launch_bounds__(128, 4) k_sweep_nodes(SweepArgs<float> s, const int* __restrict__ nodes, int count) {
+    constexpr int N = ipow(P + 1, D);
+    constexpr int NF = ipow(P + 1, D - 1);
+    constexpr int NFACE = 2 * D;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count * s.G) return;
+    const int ni = t / s.G;
+    const int g = t - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+    float A[N][N], dots[NFACE];
+    int nbrs[NFACE];
+    assemble_local<D, P, float>(s, e, a, g, A, dots, nbrs);
+    float b[N];
+    load_block<N>(s.src + node_index(s.Nw, s.G, N, e, a, g), b);
+#pragma unroll
+    for (int k = 0; k < NFACE; ++k) {
+        if (dots[k] < 0.0f && nbrs[k] >= 0) {
+            const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
+            float nb[N];
+            load_block<N>(s.psi + node_index(s.Nw, s.G, N, nbrs[k], a, g), nb);
+            // the neighbour's face values, selected in registers by the DOF map
+            float u[NF];
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) {
+                const int m = map[jj];
+                float v = nb[0];
+#pragma unroll
+                for (int c = 1; c < N; ++c) v = (m == c) ? nb[c] : v;
+                u[jj] = v;
+            }
+            const float* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
+            const float rd = -dots[k];
+#pragma unroll
+            for (int ii = 0; ii < NF; ++ii) {
+                float frow[NF];
+                load_block<NF>(F + ii * NF, frow);
+                float acc = 0.0f;
+#pragma unroll
+                for (int jj = 0; jj < NF; ++jj) acc = fmaf(frow[jj], u[jj], acc);
+                const int fi = face_dof(D, P, k, ii);
+                b[fi] = fmaf(rd, acc, b[fi]);
+            }
+        }
+    }
+    if (!solve_local<N, false>(A, b)) atomicOr(s.status, kErrSingular);
+    store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), b);
+}
+
+// RIGHT (g, a, i) FP64 <-> node-major FP32, and the node-major scattering source / moments
+static __global__ void k_right_to_nodes(int ne, int Nw, int G, int N, long long ndof, const double* __restrict__ in,
+                                 float* __restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // node-major index
+    if (t >= (long long)ne * Nw * G * N) return;
+    const int i = (int)(t % N);
+    long long r = t / N;
+    const int g = (int)(r % G); r /= G;
+    const int a = (int)(r % Nw);
+    const int e = (int)(r / Nw);
+    out[t] = (float)in[psi_index(ndof, Nw, g, a, (long long)e * N + i)];
+}
+
+static __global__ void k_nodes_to_right(int ne, int Nw, int G, int N, long long ndof, const float* __restrict__ in,
+                                 double* __restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // RIGHT index
+    if (t >= (long long)ne * Nw * G * N) return;
+    const long long s = t % ndof;
+    const long long r = t / ndof;
+    const int a = (int)(r % Nw), g = (int)(r / Nw);
+    const int e = (int)(s / N), i = (int)(s % N);
+    out[t] = (double)in[node_index(Nw, G, N, e, a, g) + i];
+}
+
+// out = (float)(D^T (S phi) + q), node-major; one thread per (cell, group, DOF)
+static __global__ void k_scatter_nodes(int ne, int Nw, int G, int N, long long ndof, double wsum,
+                                const double* __restrict__ Ms, const double* __restrict__ sigma_s,
+                                const double* __restrict__ phi, const float* qn, float* out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    const int e = (int)(s / N), i = (int)(s % N);
+    const double* M = Ms + (size_t)e * N * N + (size_t)i * N;
+    const double* ph = phi + ndof * g + (long long)e * N;
+    double acc = 0.0;
+    for (int j = 0; j < N; ++j) acc += M[j] * ph[j];
+    const double v = (sigma_s[(size_t)g * ne + e] * acc) / wsum;
+    for (int a = 0; a < Nw; ++a) {
+        const long long k = node_index(Nw, G, N, e, a, g) + i;
+        out[k] = qn ? (float)((double)qn[k] + v) : (float)v;
+    }
+}
+
+// phi(g, e N + i) = sum_a w_a psi(e, a, g, i), FP64 accumulation
+static __global__ void k_moments_nodes(int ne, int Nw, int G, int N, long long ndof, const double* __restrict__ w,
+                                const float* __restrict__ psi, double* __restrict__ phi) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    const int e = (int)(s / N), i = (int)(s % N);
+    double acc = 0.0;
+    for (int a = 0; a < Nw; ++a) acc = fma(w[a], (double)psi[node_index(Nw, G, N, e, a, g) + i], acc);
+    phi[t] = acc;
+}
+
+
+// ------------------------------------------------------------ dataflow sweep
+// One persistent launch per sweep.  The level-sorted node-groups are cut into
+// tiles of at most kTile node-groups that never span two levels; blocks take
+// tiles in order from an atomic counter.  A node-group waits only for the
+// completion flags of the upwind neighbours it reads, then computes, writes
+// psi, fences and publishes its own flag (the sweep's epoch number, so flags
+// never need clearing).  Every upwind neighbour lies in an earlier level, hence
+// in an earlier tile, which a running block has already taken: by induction
+// over the tile index every wait ends.  Waits are bounded anyway: past
+// kSpinLimit polls, or once another thread has given up, the thread records
+// kErrTimeout and goes on, so the launch always finishes.
+constexpr int kSpinLimit = 1 << 22;
+
+struct FlowArgs {
+    unsigned* flags;            // [ne * Nw * G] epoch of the last sweep that wrote each node-group
+    const unsigned* epoch;      // device word, incremented before each sweep
+    unsigned* counter;          // tile counter, zeroed before each sweep
+    const int* tile_start;      // [ntiles] first level-sorted node-group of each tile
+    const int* tile_count;      // [ntiles]
+    int ntiles;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool wait_flag(const unsigned* f, unsigned epoch, int* status, int limit = kSpinLimit) {
+    for (int it = 0;; ++it) {
+        if (ld_acquire(f) == epoch) return true;
+        if (it >= limit || (*reinterpret_cast<volatile int*>(status) & kErrTimeout)) {
+            atomicOr(status, kErrTimeout);
+            return false;
+        }
+        __nanosleep(32);
+    }
+}
+
+// Waits on a flag that nothing sets, with a caller-chosen poll limit: checks
+// that a bounded wait gives up and reports kErrTimeout.
+static __global__ void k_wait_probe(const unsigned* flag, unsigned epoch, int limit, int* status) {
+    wait_flag(flag, epoch, status, limit);
+}
+
+static __global__ void k_flow_begin(unsigned* epoch, unsigned* counter) {
+    *epoch += 1u;
+    *counter = 0u;
+}
+
+// Take the next tile: (first sorted node-group, count), or count = 0 when done.
+__device__ __forceinline__ void next_tile(const FlowArgs& f, int& start, int& count) {
+    __shared__ int s_tile;
+    __syncthreads();   // everyone has read the previous tile
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(f.counter, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= f.ntiles) { start = 0; count = 0; return; }
+    start = f.tile_start[t];
+    count = f.tile_count[t];
+}
+
+// wait for the upwind neighbours this node-group reads
+template <int D, typename R>
+__device__ __forceinline__ void wait_upwind(const FlowArgs& f, int Nw, int G, int a, int g, const R (&dots)[2 * D],
+                                            const int (&nbrs)[2 * D], unsigned epoch, int* status) {
+#pragma unroll
+    for (int k = 0; k < 2 * D; ++k)
+        if (dots[k] < R(0) && nbrs[k] >= 0)
+            wait_flag(f.flags + ((size_t)nbrs[k] * Nw + a) * G + g, epoch, status);
+}
+
+__device__ __forceinline__ void publish(const FlowArgs& f, int Nw, int G, int e, int a, int g, unsigned epoch) {
+    __threadfence();
+    st_release(f.flags + ((size_t)e * Nw + a) * G + g, epoch);
+}
+
+template <int D, typename R>
+__device__ __forceinline__ void face_info(const SweepArgs<R>& s, int e, int a, R (&dots)[2 * D], int (&nbrs)[2 * D]) {
+#pragma unroll
+    for (int k = 0; k < 2 * D; ++k) {
+        const Slot q = s.slots[(size_t)e * 2 * D + k];
+        const R d1 = s.dots[(size_t)q.face * s.Nw + a];
+        dots[k] = q.side ? -d1 : d1;
+        nbrs[k] = q.nbr;
+    }
+}
+
+// MODE 0: FP64 from stored inverses; 1: FP64 rebuilt and pivoted LU; 2: FP32 rebuilt (RIGHT layout)
+template <int D, int P, typename R, int MODE>
+__global__ void __launch_bounds__(kTile) k_flow(SweepArgs<R> s, FlowArgs f, const int* __restrict__ nodes,
+                                                const R* __restrict__ inv, long long stride) {
+    constexpr int N = ipow(P + 1, D);
+    const unsigned epoch = *f.epoch;
+    int start, count;
+    for (next_tile(f, start, count); count > 0; next_tile(f, start, count)) {
+        if ((int)threadIdx.x >= count) continue;
+        const int t = start + threadIdx.x;
+        const int ni = t / s.G;
+        const int g = t - ni * s.G;
+        const int node = nodes[ni];
+        const int e = node / s.Nw;
+        const int a = node - e * s.Nw;
+        R dots[2 * D];
+        int nbrs[2 * D];
+        R b[N];
+        if constexpr (MODE == 0) {
+            face_info<D, R>(s, e, a, dots, nbrs);
+            wait_upwind<D, R>(f, s.Nw, s.G, a, g, dots, nbrs, epoch, s.status);
+            assemble_rhs<D, P, R, true>(s, e, a, g, dots, nbrs, b);
+            const R* in = inv + t;
+            R x[N];
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                R acc = R(0);
+#pragma unroll
+                for (int j = 0; j < N; ++j) acc = fma_r(__ldg(in + (size_t)(i * N + j) * stride), b[j], acc);
+                x[i] = acc;
+            }
+            store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), x);
+        } else {
+            R A[N][N];
+            assemble_local<D, P, R>(s, e, a, g, A, dots, nbrs);
+            wait_upwind<D, R>(f, s.Nw, s.G, a, g, dots, nbrs, epoch, s.status);
+            assemble_rhs<D, P, R, true>(s, e, a, g, dots, nbrs, b);
+            if (!solve_local<N, MODE == 1>(A, b)) atomicOr(s.status, kErrSingular);
+            store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), b);
+        }
+        publish(f, s.Nw, s.G, e, a, g, epoch);
+    }
+}
+
+// FP32, node-major layout, local systems rebuilt each sweep
+template <int D, int P>
+__global__ void __launch_bounds__(kTile, 4) k_flow_nodes(SweepArgs<float> s, FlowArgs f, const int* __restrict__ nodes) {
+    constexpr int N = ipow(P + 1, D);
+    constexpr int NF = ipow(P + 1, D - 1);
+    constexpr int NFACE = 2 * D;
+    const unsigned epoch = *f.epoch;
+    int start, count;
+    for (next_tile(f, start, count); count > 0; next_tile(f, start, count)) {
+        if ((int)threadIdx.x >= count) continue;
+        const int t = start + threadIdx.x;
+        const int ni = t / s.G;
+        const int g = t - ni * s.G;
+        const int node = nodes[ni];
+        const int e = node / s.Nw;
+        const int a = node - e * s.Nw;
+        float A[N][N], dots[NFACE];
+        int nbrs[NFACE];
+        assemble_local<D, P, float>(s, e, a, g, A, dots, nbrs);
+        float b[N];
+        load_block<N>(s.src + node_index(s.Nw, s.G, N, e, a, g), b);
+        wait_upwind<D, float>(f, s.Nw, s.G, a, g, dots, nbrs, epoch, s.status);
+#pragma unroll
+        for (int k = 0; k < NFACE; ++k) {
+            if (dots[k] < 0.0f && nbrs[k] >= 0) {
+                const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
+                const float* up = s.psi + node_index(s.Nw, s.G, N, nbrs[k], a, g);
+                float nb[N];
+#pragma unroll
+                for (int c = 0; c < N; ++c) nb[c] = __ldcg(up + c);
+                float u[NF];
+#pragma unroll
+                for (int jj = 0; jj < NF; ++jj) {
+                    const int m = map[jj];
+                    float v = nb[0];
+#pragma unroll
+                    for (int c = 1; c < N; ++c) v = (m == c) ? nb[c] : v;
+                    u[jj] = v;
+                }
+                const float* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
+                const float rd = -dots[k];
+#pragma unroll
+                for (int ii = 0; ii < NF; ++ii) {
+                    float frow[NF];
+                    load_block<NF>(F + ii * NF, frow);
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int jj = 0; jj < NF; ++jj) acc = fmaf(frow[jj], u[jj], acc);
+                    const int fi = face_dof(D, P, k, ii);
+                    b[fi] = fmaf(rd, acc, b[fi]);
+                }
+            }
+        }
+        if (!solve_local<N, false>(A, b)) atomicOr(s.status, kErrSingular);
+        store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), b);
+        publish(f, s.Nw, s.G, e, a, g, epoch);
+    }
 }
 
 // y = L x (AdvectionOperator::Mult, src/sweep.cpp:1246-1387) from the cell's

@@ -42,7 +42,7 @@ cudaError_t factor_all(Handle& h, const SweepArgs<double>& args) {
     constexpr int kBlock = 128;
     const long long total = (long long)h.G * h.ne * h.Nw;
     const unsigned grid = (unsigned)((total + kBlock - 1) / kBlock);
-    k_factor_all<D, P><<<grid, kBlock, 0, h.stream>>>(args, h.d_level_nodes, total, h.d_inv, h.f_inv);
+    k_factor_all<D, P><<<grid, kBlock, 0, h.stream>>>(args, h.d_level_nodes, total, h.d_inv);
     return cudaGetLastError();
 }
 
@@ -69,6 +69,51 @@ cudaError_t cached_dispatch(Handle& h, const SweepArgs<R>& a, const R* inv, cuda
         case 11: return sweep_levels_cached<1, 1, R>(h, a, inv, st);
         case 21: return sweep_levels_cached<2, 1, R>(h, a, inv, st);
         case 31: return sweep_levels_cached<3, 1, R>(h, a, inv, st);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+// Dataflow launch: epoch bump + counter reset, then one persistent grid sized
+// to the blocks that fit the GPU at once.
+template <typename Kernel, typename... Args>
+cudaError_t launch_flow(Handle& h, cudaStream_t stream, Kernel kernel, size_t smem, Args... args) {
+    static int max_blocks = 0;   // per kernel instantiation
+    if (max_blocks == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTile, smem);
+        if (e != cudaSuccess) return e;
+        max_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    }
+    k_flow_begin<<<1, 1, 0, stream>>>(h.d_flow_words, h.d_flow_words + 1);
+    const int grid = h.ntiles < max_blocks ? h.ntiles : max_blocks;
+    kernel<<<grid > 0 ? grid : 1, kTile, smem, stream>>>(args...);
+    return cudaGetLastError();
+}
+
+inline FlowArgs flow_args(Handle& h) {
+    FlowArgs f;
+    f.flags = h.d_flags;
+    f.epoch = h.d_flow_words;
+    f.counter = h.d_flow_words + 1;
+    f.tile_start = h.d_tile_start;
+    f.tile_count = h.d_tile_count;
+    f.ntiles = h.ntiles;
+    return f;
+}
+
+template <int MODE, typename R>
+cudaError_t flow_dispatch(Handle& h, const SweepArgs<R>& a, const R* inv, cudaStream_t st) {
+    const long long stride = (long long)h.G * h.ne * h.Nw;
+    const FlowArgs f = flow_args(h);
+    switch (h.dim * 10 + h.p) {
+        case 10: return launch_flow(h, st, k_flow<1, 0, R, MODE>, 0, a, f, h.d_level_nodes, inv, stride);
+        case 11: return launch_flow(h, st, k_flow<1, 1, R, MODE>, 0, a, f, h.d_level_nodes, inv, stride);
+        case 20: return launch_flow(h, st, k_flow<2, 0, R, MODE>, 0, a, f, h.d_level_nodes, inv, stride);
+        case 21: return launch_flow(h, st, k_flow<2, 1, R, MODE>, 0, a, f, h.d_level_nodes, inv, stride);
+        case 30: return launch_flow(h, st, k_flow<3, 0, R, MODE>, 0, a, f, h.d_level_nodes, inv, stride);
+        case 31: return launch_flow(h, st, k_flow<3, 1, R, MODE>, 0, a, f, h.d_level_nodes, inv, stride);
         default: return cudaErrorNotSupported;
     }
 }

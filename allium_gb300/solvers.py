@@ -27,8 +27,8 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from .sweep import (DiscreteToMoment, InverseAdvectionOperator, MomentsF32, ScatteringSource,
-                    ScatteringSourceF32)
+from .sweep import (DiscreteToMoment, InverseAdvectionOperator, MomentsF32, MomentsF32Nodes, ScatteringSource,
+                    ScatteringSourceF32, ScatteringSourceF32Nodes)
 
 
 class SchurOperator:
@@ -64,6 +64,18 @@ class SchurOperator:
         return out
 
     def apply32(self, x, out):
+        """T with the FP32 sweep on node-major vectors (contiguous runs per level)."""
+        if self.psi32 is None:
+            self.psi32 = torch.empty(self.L.width, dtype=torch.float32, device=self.psi.device)
+        ScatteringSourceF32Nodes(self.L, self.sigma_s, x, None, self.psi32)
+        self.L.MultF32Nodes(self.psi32, self.psi32)
+        self.sweeps32 += 1
+        MomentsF32Nodes(self.L, self.psi32, self.tmp)
+        torch.sub(x, self.tmp, out=out)
+        return out
+
+    def apply32_right(self, x, out):
+        """T with the FP32 sweep on allium's RIGHT layout."""
         if self.psi32 is None:
             self.psi32 = torch.empty(self.L.width, dtype=torch.float32, device=self.psi.device)
         ScatteringSourceF32(self.L, self.sigma_s, x, None, self.psi32)

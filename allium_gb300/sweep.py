@@ -123,9 +123,28 @@ class InverseAdvectionOperator:
         check(_lib.lib().allium_sweep_mult_f32(self.h, C.c_void_p(_ptr(source, np.float32, self.width, "source")),
                                                C.c_void_p(_ptr(psi, np.float32, self.height, "psi"))), self.h)
 
+    def SetSchedule(self, mode):
+        """0: one launch per wavefront level (default); 1: one persistent dataflow launch per sweep."""
+        check(_lib.lib().allium_sweep_set_schedule(self.h, int(mode)), self.h)
+
     def SetFactorCache(self, mode):
         """1: keep FP64 local-matrix inverses across Mults when memory allows (default); 0: off."""
         check(_lib.lib().allium_sweep_set_factor_cache(self.h, int(mode)), self.h)
+
+    def MultF32Nodes(self, source, psi):
+        """FP32 sweep on node-major device vectors v[((e*Nw + a)*G + g)*n + i]."""
+        check(_lib.lib().allium_sweep_mult_f32_nodes(self.h, C.c_void_p(_ptr(source, np.float32, self.width, "source")),
+                                                     C.c_void_p(_ptr(psi, np.float32, self.height, "psi"))), self.h)
+
+    def ToNodeLayoutF32(self, psi, out):
+        check(_lib.lib().allium_sweep_to_node_layout_f32(self.h, C.c_void_p(_ptr(psi, np.float64, self.width, "psi")),
+                                                         C.c_void_p(_ptr(out, np.float32, self.width, "out"))), self.h)
+        return out
+
+    def FromNodeLayoutF32(self, v, psi):
+        check(_lib.lib().allium_sweep_from_node_layout_f32(self.h, C.c_void_p(_ptr(v, np.float32, self.width, "v")),
+                                                           C.c_void_p(_ptr(psi, np.float64, self.width, "psi"))), self.h)
+        return psi
 
     def AssembleLocalMatrices(self, sigma_t=None):
         if sigma_t is None:
@@ -237,6 +256,23 @@ def ScatteringSourceF32(Linv: InverseAdvectionOperator, sigma_s, phi, q_fixed, o
         Linv.h, C.c_void_p(sig.ctypes.data), C.c_void_p(_ptr(phi, np.float64, Linv.G * Linv.ndof, "phi")),
         C.c_void_p(qp), C.c_void_p(_ptr(out, np.float32, Linv.width, "out"))), Linv.h)
     return out
+
+
+def ScatteringSourceF32Nodes(Linv: InverseAdvectionOperator, sigma_s, phi, q_nodes, out):
+    """Node-major FP32 out = D^T (S phi) + q_nodes; device tensors only."""
+    sig = np.ascontiguousarray(sigma_s, dtype=np.float64).reshape(Linv.G, -1)
+    qp = _ptr(q_nodes, np.float32, Linv.width, "q_nodes") if q_nodes is not None else None
+    check(_lib.lib().allium_sweep_scattering_source_f32_nodes(
+        Linv.h, C.c_void_p(sig.ctypes.data), C.c_void_p(_ptr(phi, np.float64, Linv.G * Linv.ndof, "phi")),
+        C.c_void_p(qp), C.c_void_p(_ptr(out, np.float32, Linv.width, "out"))), Linv.h)
+    return out
+
+
+def MomentsF32Nodes(Linv: InverseAdvectionOperator, psi, phi):
+    """FP64 zeroth moment of a node-major FP32 psi; device tensors only."""
+    check(_lib.lib().allium_sweep_moments_f32_nodes(Linv.h, C.c_void_p(_ptr(psi, np.float32, Linv.width, "psi")),
+                                                    C.c_void_p(_ptr(phi, np.float64, Linv.G * Linv.ndof, "phi"))), Linv.h)
+    return phi
 
 
 def MomentsF32(Linv: InverseAdvectionOperator, psi, phi):

@@ -137,7 +137,15 @@ int allium_sweep_mult(allium_sweep* s, const double* source, double* psi);
  * factoring.  mode 0: never cache (frees the cache). */
 int allium_sweep_set_factor_cache(allium_sweep* s, int mode);
 
-/* The same sweep with FP32 storage and FP32 local solves (unpivoted
+/* Launch schedule of the sweep (no counterpart in the reference).
+ * 0 (default): one launch per wavefront level (the reference's frontier
+ * order), replayed as a CUDA graph.
+ * 1: one persistent launch per sweep; each (cell, angle, group) waits on
+ * completion flags of the upwind neighbours it reads, so later wavefronts
+ * start while earlier ones drain (orders p <= 1).  Same results bit for bit. */
+int allium_sweep_set_schedule(allium_sweep* s, int mode);
+
+/* The same sweep with FP32 storage and FP32 local solves rebuilt every call (unpivoted
  * elimination; the local upwind matrix has a positive definite symmetric part
  * when sigma_t > 0).  Meant as the inner operator of an FP64 outer iteration. */
 int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi);
@@ -195,9 +203,29 @@ int allium_sweep_moments_f32(allium_sweep* s, const float* psi, double* phi);
 int allium_sweep_scattering_source_f32(allium_sweep* s, const double* sigma_s, const double* phi,
                                        const float* q_fixed, float* out);
 
+/* Node-major FP32 companions for inner iterations the caller keeps on the GPU
+ * (no counterpart in the reference; device vectors only).  The node-major
+ * layout stores v[((e*Nw + a)*G + g)*n + i]: in a wavefront level the
+ * consecutive angles of one cell, and their upwind traces, are contiguous.
+ * Conversions to/from allium's RIGHT FP64 layout, the FP32 sweep (in place
+ * allowed; local systems in FP32, unpivoted), the scattering source
+ * D^T (S phi) + q (S phi in FP64) and the FP64-accumulated zeroth moment. */
+int allium_sweep_to_node_layout_f32(allium_sweep* s, const double* psi_right, float* out_nodes);
+int allium_sweep_from_node_layout_f32(allium_sweep* s, const float* in_nodes, double* psi_right);
+int allium_sweep_mult_f32_nodes(allium_sweep* s, const float* source, float* psi);
+int allium_sweep_scattering_source_f32_nodes(allium_sweep* s, const double* sigma_s, const double* phi,
+                                             const float* q_nodes, float* out);
+int allium_sweep_moments_f32_nodes(allium_sweep* s, const float* psi, double* phi);
+
 /* Wavefront level of every (cell, angle) node e*Nw + a (the Kahn frontier
  * index of src/sweep.cpp:308-512), host or device int array [Ne*Nw]. */
 int allium_sweep_levels(allium_sweep* s, int* levels);
+
+/* Failure-detection self test (no counterpart in the reference): runs the
+ * sweep's bounded device wait on a completion flag that nothing sets, with
+ * poll_limit polls (1..2^20); the wait gives up and the call returns
+ * ALLIUM_ERR_TIMEOUT with the device still usable. */
+int allium_sweep_selftest_wait(allium_sweep* s, int poll_limit);
 
 /* Wait for the handle's stream; report sticky kernel errors and clear them. */
 int allium_sweep_synchronize(allium_sweep* s);

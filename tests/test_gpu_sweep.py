@@ -75,6 +75,16 @@ def test_sweep_parity(case):
     L.synchronize()
     assert rel_err(f.cpu().numpy(), ref) < TOL32
 
+    # FP32 sweep in the node-major layout
+    if case[2] == 1:
+        fn = torch.empty(o.psi_size, dtype=torch.float32, device="cuda")
+        L.ToNodeLayoutF32(torch.from_numpy(src).cuda(), fn)
+        L.MultF32Nodes(fn, fn)
+        back64 = torch.empty(o.psi_size, dtype=torch.float64, device="cuda")
+        L.FromNodeLayoutF32(fn, back64)
+        L.synchronize()
+        assert rel_err(back64.cpu().numpy(), ref) < TOL32
+
     # forward operator and L L^{-1} = I
     y = np.empty_like(src)
     AdvectionOperator(L).Mult(src, y)
@@ -276,6 +286,47 @@ def test_cycle_is_reported():
     with pytest.raises(AlliumError) as e:
         InverseAdvectionOperator(mesh, 1, quad, sig)
     assert e.value.status == 2
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c[2] <= 1], ids=[f"d{c[0]}p{c[2]}S{c[3]}G{c[4]}" for c in CASES if c[2] <= 1])
+def test_schedules_agree(case):
+    # the persistent dataflow launch and one launch per level run the same
+    # per-node arithmetic: results are identical bit for bit
+    mesh, quad, sig, o, L = build(*case)
+    src = torch.from_numpy(np.random.default_rng(6).random(o.psi_size)).cuda()
+    outs = {}
+    for sched in (0, 1):
+        L.SetSchedule(sched)
+        for cache in (0, 1):
+            L.SetFactorCache(cache)
+            y = torch.empty_like(src)
+            L.Mult(src, y)
+            y32 = torch.empty(o.psi_size, dtype=torch.float32, device="cuda")
+            L.MultF32(src.float(), y32)
+            yn = torch.empty_like(y32)
+            L.ToNodeLayoutF32(src, yn)
+            L.MultF32Nodes(yn, yn)
+            L.synchronize()
+            outs[(sched, cache)] = (y.cpu().numpy(), y32.cpu().numpy(), yn.cpu().numpy())
+    for cache in (0, 1):
+        for k in range(3):
+            assert np.array_equal(outs[(0, cache)][k], outs[(1, cache)][k])
+    assert rel_err(outs[(1, 1)][0], o.mult(src.cpu().numpy())) < TOL64
+
+
+def test_bounded_wait_reports_timeout():
+    # failure detection without a GPU fault: a wait on a flag nothing sets gives
+    # up after its poll limit, the call returns TIMEOUT and the device still works
+    mesh, quad, sig = problem(2, (6, 6), 1)
+    L = InverseAdvectionOperator(mesh, 1, quad, sig)
+    from allium_gb300 import _lib
+    st = _lib.lib().allium_sweep_selftest_wait(L.h, 1000)
+    assert st == 4
+    src = np.random.default_rng(1).random(L.width)
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    o = OracleSweep(mesh, 1, quad, sig)
+    assert rel_err(psi, o.mult(src)) < TOL64
 
 
 def test_errors_are_reported():
