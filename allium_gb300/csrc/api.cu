@@ -65,7 +65,7 @@ void free_all(Handle& h) {
     void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
-                    h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count};
+                    h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -577,6 +577,36 @@ int allium_sweep_selftest_wait(allium_sweep* s, int poll_limit) {
     Handle& h = s->h;
     CUDA_OR_FAIL(h, allium::launch_wait_probe(h, poll_limit));
     return check_status(h);
+}
+
+int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum) {
+    if (!s || kind < 0) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (kind > 2) { h.last_error = "only the zero (1) and zero-and-scale (2) fixups are implemented"; return ALLIUM_ERR_UNSUPPORTED; }
+    if (kind && h.n > 8) { h.last_error = "the fixup is implemented for local systems up to 8 x 8"; return ALLIUM_ERR_UNSUPPORTED; }
+    if (!h.d_fix_counts) {
+        CUDA_OR_FAIL(h, cudaMalloc(&h.d_fix_counts, 2 * sizeof(unsigned long long)));
+        CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_fix_counts, 0, 2 * sizeof(unsigned long long), h.stream));
+    }
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    allium::drop_graphs(h);   // captured launches carry the fixup settings
+    h.fix_kind = kind;
+    h.fix_min = minimum;
+    return ALLIUM_OK;
+}
+
+int allium_sweep_fixup_counts(allium_sweep* s, long long* applied, long long* failed, int reset) {
+    if (!s) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    unsigned long long c[2] = {0, 0};
+    if (h.d_fix_counts) {
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(c, h.d_fix_counts, sizeof(c), cudaMemcpyDeviceToHost, h.stream));
+        if (reset) CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_fix_counts, 0, sizeof(c), h.stream));
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    }
+    if (applied) *applied = (long long)c[0];
+    if (failed) *failed = (long long)c[1];
+    return ALLIUM_OK;
 }
 
 int allium_sweep_synchronize(allium_sweep* s) {

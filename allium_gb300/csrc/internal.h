@@ -86,6 +86,11 @@ struct Handle {
     cudaStream_t capture_stream = nullptr;
     bool use_graphs = true;
 
+    // negative-flux fixup
+    int fix_kind = 0;
+    double fix_min = 0.0;
+    unsigned long long* d_fix_counts = nullptr;
+
     // dataflow schedule (one persistent launch per sweep)
     int schedule = 0;                // 0: one launch per wavefront level, 1: dataflow
     unsigned* d_flags = nullptr;     // [ne * Nw * G]

@@ -10,7 +10,8 @@ cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi) {
     a.Gm = h.f_G; a.M = h.f_M; a.Mt = h.f_Mt; a.F = h.f_F; a.sigma = h.f_sigma;
     a.tau = (float)h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status;
-    if (h.schedule == 1 && h.p <= 1) {
+    a.fix_kind = h.fix_kind; a.fix_min = (float)h.fix_min; a.fix_counts = h.d_fix_counts;
+    if (h.schedule == 1 && h.p <= 1 && !h.fix_kind) {
         cudaError_t e = prepare_flow(h);
         if (e != cudaSuccess) return e;
         return run_graph(h, 13, src, psi, [&](cudaStream_t st) { return flow_dispatch<2, float>(h, a, nullptr, st); });
@@ -40,6 +41,7 @@ cudaError_t launch_sweep_nodes_f32(Handle& h, const float* src, float* psi) {
     a.Gm = h.f_G; a.M = h.f_M; a.Mt = h.f_Mt; a.F = h.f_F; a.sigma = h.f_sigma;
     a.tau = (float)h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status;
+    a.fix_kind = h.fix_kind; a.fix_min = (float)h.fix_min; a.fix_counts = h.d_fix_counts;
     if (h.schedule == 1) {
         cudaError_t e = prepare_flow(h);
         if (e != cudaSuccess) return e;

@@ -39,7 +39,45 @@ struct SweepArgs {
     const R* src;
     R* psi;
     int* status;
+    // negative-flux fixup (src/fixup.cpp): 0 none, 1 zero, 2 zero and scale
+    int fix_kind;
+    R fix_min;
+    unsigned long long* fix_counts;   // [0] applied, [1] failed
 };
+
+// ZeroFixupOperator / ZeroAndScaleFixupOperator::Apply (src/fixup.cpp:3-57) on
+// the solved local vector x, with w the column sums of the local matrix and
+// balance = sum of the right-hand side.  Returns 0 (untouched), 1 or -1.
+template <int N, typename R>
+__device__ __forceinline__ int apply_fixup(int kind, R xmin, const R (&w)[N], R balance, R (&x)[N]) {
+    R lo = x[0];
+#pragma unroll
+    for (int i = 1; i < N; ++i) lo = x[i] < lo ? x[i] : lo;
+    if (kind == 1) {
+        int applied = 0;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (x[i] <= xmin) { x[i] = xmin; applied = 1; }
+        return applied;
+    }
+    if (lo > xmin) return 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        if (x[i] <= xmin) x[i] = xmin;
+    R nb = R(0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) nb += w[i] * x[i];
+    if (balance < R(0) || nb < R(0)) return -1;
+    if (balance == R(0) || nb == R(0)) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = R(0);
+    } else {
+        const R sc = balance / nb;
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] *= sc;
+    }
+    return 1;
+}
 
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
@@ -330,7 +368,22 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 4 : 1)) k_sweep_level(S
     assemble_local<D, P, R>(s, e, a, g, A, dots, nbrs);
     R b[N];
     assemble_rhs<D, P, R>(s, e, a, g, dots, nbrs, b);
+    R w[N], balance = R(0);
+    if (s.fix_kind) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            R c = R(0);
+#pragma unroll
+            for (int j = 0; j < N; ++j) c += A[j][i];
+            w[i] = c;
+            balance += b[i];
+        }
+    }
     if (!solve_local<N, PIVOT>(A, b)) atomicOr(s.status, kErrSingular);
+    if (s.fix_kind) {
+        const int r = apply_fixup<N, R>(s.fix_kind, s.fix_min, w, balance, b);
+        if (r) atomicAdd(s.fix_counts + (r > 0 ? 0 : 1), 1ull);
+    }
     store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), b);
 }
 

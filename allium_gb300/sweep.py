@@ -123,6 +123,20 @@ class InverseAdvectionOperator:
         check(_lib.lib().allium_sweep_mult_f32(self.h, C.c_void_p(_ptr(source, np.float32, self.width, "source")),
                                                C.c_void_p(_ptr(psi, np.float32, self.height, "psi"))), self.h)
 
+    def SetFixup(self, kind, minimum=0.0):
+        """Negative-flux fixup: None/0 off, "zero"/1, "zero_and_scale"/2 (src/fixup.cpp:3-57)."""
+        kinds = {None: 0, "none": 0, "zero": 1, "zero_and_scale": 2}
+        k = kinds[kind] if not isinstance(kind, int) else kind
+        check(_lib.lib().allium_sweep_set_fixup(self.h, k, float(minimum)), self.h)
+
+    def UseFixup(self, use=True, kind="zero_and_scale", minimum=0.0):
+        self.SetFixup(kind if use else 0, minimum)
+
+    def FixupCounts(self, reset=False):
+        a, f = C.c_longlong(), C.c_longlong()
+        check(_lib.lib().allium_sweep_fixup_counts(self.h, C.byref(a), C.byref(f), int(reset)), self.h)
+        return a.value, f.value
+
     def SetSchedule(self, mode):
         """0: one launch per wavefront level (default); 1: one persistent dataflow launch per sweep."""
         check(_lib.lib().allium_sweep_set_schedule(self.h, int(mode)), self.h)

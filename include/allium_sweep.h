@@ -150,6 +150,18 @@ int allium_sweep_set_schedule(allium_sweep* s, int mode);
  * when sigma_t > 0).  Meant as the inner operator of an FP64 outer iteration. */
 int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi);
 
+/* Negative-flux fixup inside the sweep (SetFixupOperator / UseFixup,
+ * src/sweep.hpp:108-117, applied at src/sweep.cpp:465-470): kind 0 off,
+ * 1 ZeroFixupOperator, 2 ZeroAndScaleFixupOperator (src/fixup.cpp:3-57),
+ * with the operator's minimum_solution.  The local-optimization and
+ * "Ryosuke" fixups return ALLIUM_ERR_UNSUPPORTED, as do systems above 8 x 8.
+ * While a fixup is on, Mult rebuilds and factors every local system. */
+int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum);
+
+/* Number of local solves the fixup changed (applied) or could not balance
+ * (failed, Apply returned -1) since the last reset; reset != 0 zeroes them. */
+int allium_sweep_fixup_counts(allium_sweep* s, long long* applied, long long* failed, int reset);
+
 /* AdvectionOperator::Mult (src/sweep.cpp:1246-1387): y = L x, FP64. x != y. */
 int allium_sweep_apply_L(allium_sweep* s, const double* x, double* y);
 

@@ -41,6 +41,8 @@ def lib():
         L.oracle_moments.argtypes = [vp, dp, dp, C.c_int]
         L.oracle_moments_transpose.argtypes = [vp, dp, dp, C.c_int, C.c_double, C.c_int]
         L.oracle_form_source.argtypes = [vp, dp, FN, dp, C.c_int, FN, dp]
+        L.oracle_set_fixup.argtypes = [vp, C.c_int, C.c_double]
+        L.oracle_fixup_counts.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.oracle_scattering_source.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_l2_error.argtypes = [vp, dp, C.c_int, C.c_int, FN]
         L.oracle_l2_error.restype = C.c_double
@@ -97,6 +99,14 @@ class OracleSweep:
 
     def set_time_absorption(self, tau):
         lib().oracle_set_time_absorption(self.h, float(tau))
+
+    def set_fixup(self, kind, minimum=0.0):
+        lib().oracle_set_fixup(self.h, int(kind), float(minimum))
+
+    def fixup_counts(self):
+        a, f = C.c_longlong(), C.c_longlong()
+        lib().oracle_fixup_counts(self.h, C.byref(a), C.byref(f))
+        return a.value, f.value
 
     def levels(self):
         lev = np.zeros(self.ne * self.Nw, dtype=np.int32)

@@ -153,6 +153,8 @@ struct Oracle {
     std::vector<double> omega, wq; double wsum;
     std::vector<double> sigma;  // [G][ne]
     bool timedep = false; double tau = 0.0;
+    int fix_kind = 0; double fix_min = 0.0;        // negative-flux fixup (fixup.cpp)
+    long long fix_applied = 0, fix_failed = 0;
     std::vector<double> basis_nodes;
     std::vector<double> Ms, Gm, Mt, F;  // see assemble()
     std::vector<int> indeg0;            // in-degree per node
@@ -565,7 +567,31 @@ bool solve_node(const Oracle& o, int e, int a, const double* src, double* psi,
             for (int i = 0; i < n; ++i)
                 for (int j = 0; j < n; ++j) A[i + j * n] += o.tau * Mt[i * n + j];
         }
+        std::vector<double> Acopy, bcopy;
+        if (o.fix_kind) { Acopy = A; bcopy = rhs; }
         if (!linear_solve(n, A.data(), rhs.data())) return false;
+        if (o.fix_kind) {
+            // ZeroFixupOperator / ZeroAndScaleFixupOperator::Apply (fixup.cpp:3-57)
+            int applied = 0;
+            double lo = rhs[0];
+            for (int i = 1; i < n; ++i) lo = std::min(lo, rhs[i]);
+            if (o.fix_kind == 1) {
+                for (int i = 0; i < n; ++i) if (rhs[i] <= o.fix_min) { rhs[i] = o.fix_min; applied = 1; }
+            } else if (!(lo > o.fix_min)) {
+                std::vector<double> w(n, 0.0);
+                for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) w[i] += Acopy[j + i * n];
+                for (int i = 0; i < n; ++i) if (rhs[i] <= o.fix_min) rhs[i] = o.fix_min;
+                double orig = 0.0, nb = 0.0;
+                for (int i = 0; i < n; ++i) { orig += bcopy[i]; nb += w[i] * rhs[i]; }
+                if (orig < 0.0 || nb < 0.0) applied = -1;
+                else if (orig == 0.0 || nb == 0.0) { for (int i = 0; i < n; ++i) rhs[i] = 0.0; applied = 1; }
+                else { for (int i = 0; i < n; ++i) rhs[i] *= orig / nb; applied = 1; }
+            }
+            if (applied) {
+#pragma omp atomic
+                (applied > 0 ? const_cast<Oracle&>(o).fix_applied : const_cast<Oracle&>(o).fix_failed) += 1;
+            }
+        }
         for (int i = 0; i < n; ++i) psi[pidx(o, g, a, off + i)] = rhs[i];
     }
     return true;
@@ -608,6 +634,16 @@ void oracle_set_time_absorption(void* h, double tau) {
     Oracle& o = *static_cast<Oracle*>(h);
     o.tau = tau; o.timedep = true;
     if (o.Mt.empty()) assemble_time_mass(o);
+}
+
+void oracle_set_fixup(void* h, int kind, double minimum) {
+    Oracle& o = *static_cast<Oracle*>(h);
+    o.fix_kind = kind; o.fix_min = minimum; o.fix_applied = o.fix_failed = 0;
+}
+
+void oracle_fixup_counts(void* h, long long* applied, long long* failed) {
+    const Oracle& o = *static_cast<Oracle*>(h);
+    *applied = o.fix_applied; *failed = o.fix_failed;
 }
 
 int oracle_num_faces(void* h) { return (int)static_cast<Oracle*>(h)->faces.size(); }

@@ -329,6 +329,42 @@ def test_bounded_wait_reports_timeout():
     assert rel_err(psi, o.mult(src)) < TOL64
 
 
+@pytest.mark.parametrize("dim,cells", [(2, (16, 16)), (3, (8, 8, 8))])
+@pytest.mark.parametrize("kind", [1, 2])
+def test_fixup_parity(dim, cells, kind):
+    # optically thick cells next to a point source: p = 1 DG fluxes dip below
+    # zero; the zero (1) and zero-and-scale (2) fixups of src/fixup.cpp remove them
+    mesh = M.cartesian(cells, jitter=0.1, seed=2)
+    quad = Q.level_symmetric(4, dim)
+    sig = np.full((2, mesh.num_elements), 50.0)
+    sig[1] *= 0.2
+    q = np.zeros((2, mesh.num_elements))
+    q[:, 0] = 100.0
+    o = OracleSweep(mesh, 1, quad, sig)
+    L = InverseAdvectionOperator(mesh, 1, quad, sig)
+    src = FormTransportSource(L, q)
+    plain = np.empty_like(src)
+    L.Mult(src, plain)
+    assert plain.min() < 0
+    o.set_fixup(kind, 0.0)
+    L.SetFixup(kind, 0.0)
+    ref = o.mult(src)
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert psi.min() >= 0.0
+    assert rel_err(psi, ref) < 1e-11
+    applied, failed = L.FixupCounts(reset=True)
+    ra, rf = o.fixup_counts()
+    assert abs(applied - ra) <= max(3, ra // 100) and failed == rf
+    f32 = torch.from_numpy(src.astype(np.float32)).cuda()
+    L.MultF32(f32, f32)
+    L.synchronize()
+    assert f32.min().item() >= 0.0
+    L.SetFixup(0)
+    L.Mult(src, psi)
+    assert np.array_equal(psi, plain)
+
+
 def test_errors_are_reported():
     mesh, quad, sig = problem(2, (4, 4), 1)
     with pytest.raises(AlliumError) as e:
