@@ -65,7 +65,8 @@ void free_all(Handle& h) {
     void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
-                    h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts};
+                    h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts,
+                    h.d_refl, h.d_feed};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -111,9 +112,12 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
         fe->lump < 0 || fe->lump > 7)
         return ALLIUM_ERR_UNSUPPORTED;
     if (mesh->dim == 3 && fe->order > 2) return ALLIUM_ERR_UNSUPPORTED;   // 64 x 64 local systems
+    std::vector<int> refl_attrs;
     if (bc)
-        for (int i = 0; i < bc->num; ++i)
-            if (bc->kinds[i] != ALLIUM_BC_INFLOW) return ALLIUM_ERR_UNSUPPORTED;
+        for (int i = 0; i < bc->num; ++i) {
+            if (bc->kinds[i] == ALLIUM_BC_REFLECTIVE) refl_attrs.push_back(bc->attributes[i]);
+            else if (bc->kinds[i] != ALLIUM_BC_INFLOW) return ALLIUM_ERR_ARG;
+        }
 
     allium_sweep* s = new allium_sweep;
     Handle& h = s->h;
@@ -138,6 +142,7 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     allium::Topology topo;
     int st = allium::build_topology(*mesh, h.p, topo, h.last_error);
     if (st != ALLIUM_OK) return fail(st);
+    allium::mark_reflective(topo, h.nface, refl_attrs);
     h.nfaces = topo.nfaces;
 
     if (cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -170,6 +175,7 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     CSTEP(cudaMalloc(&h.d_scratch, (h.scratch_len + 1) * sizeof(double)));
     CSTEP(allium::launch_face_normals(h));
     CSTEP(allium::launch_face_dots(h));
+    STEP(allium::compute_reflections(h, topo.refl_faces));
     CSTEP(allium::launch_assemble(h));
     STEP(allium::compute_levels(h));
     CSTEP(cudaStreamSynchronize(h.stream));
@@ -488,6 +494,7 @@ int allium_sweep_mult_f32_nodes(allium_sweep* s, const float* source, float* psi
     Handle& h = s->h;
     if (int st = device_only(h, {source, psi}, "allium_sweep_mult_f32_nodes")) return st;
     if (misaligned(source, psi, true, true)) { h.last_error = "device vectors must be 16-byte aligned"; return ALLIUM_ERR_ARG; }
+    if (h.nrefl) { h.last_error = "the node layout sweep supports inflow boundaries only"; return ALLIUM_ERR_UNSUPPORTED; }
     if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
     CUDA_OR_FAIL(h, allium::launch_sweep_nodes_f32(h, source, psi));
     return ALLIUM_OK;

@@ -25,8 +25,9 @@ struct RefTables {
     double rx[6][kMaxRule], rw[6][kMaxRule];
 };
 
-// Per (cell, local face) topology.  face < 0 never happens; nbr < 0 on the
-// boundary.  side = 0 when the cell is the face's element 1 (lower index).
+// Per (cell, local face) topology.  nbr >= 0: interior face; nbr = -1:
+// inflow/vacuum boundary; nbr = -2 - c: reflective boundary face number c.
+// side = 0 when the cell is the face's element 1 (lower index).
 struct Slot {
     int face, nbr, side, attr;
 };
@@ -85,6 +86,11 @@ struct Handle {
     int graph_next = 0;
     cudaStream_t capture_stream = nullptr;
     bool use_graphs = true;
+
+    // reflective boundaries: reflected angle of each angle at reflective face c
+    int nrefl = 0;
+    int* d_refl = nullptr;           // [nrefl][Nw] reflected angle feeding each entering angle
+    int* d_feed = nullptr;           // [nrefl][Nw] entering angle fed by each angle
 
     // negative-flux fixup
     int fix_kind = 0;
@@ -153,13 +159,16 @@ struct Topology {
     std::vector<Slot> slots;          // [ne][2 dim]
     std::vector<uint8_t> nbrmap;      // [ne][2 dim][nf]
     std::vector<double> corners;      // [ne][2^dim][dim], corner order c = c0 + 2 c1 + 4 c2
+    std::vector<int> refl_faces;      // face id of reflective boundary face c
 };
 int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string& err);
+void mark_reflective(Topology& t, int nface, const std::vector<int>& refl_attrs);
 
 // ---- setup kernels (setup.cu)
 cudaError_t launch_face_normals(Handle& h);
 cudaError_t launch_face_dots(Handle& h);
 cudaError_t launch_assemble(Handle& h);
+int compute_reflections(Handle& h, const std::vector<int>& refl_faces);   // allium status
 cudaError_t launch_time_mass(Handle& h);
 int compute_levels(Handle& h);   // returns an allium status
 cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out);

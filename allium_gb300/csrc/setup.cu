@@ -156,6 +156,71 @@ cudaError_t launch_face_dots(Handle& h) {
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ reflections
+// GetReflectedAngleIndex (src/angular_quadrature.cpp:27-36, GetIndexForAngle
+// :8-25) for every angle entering the domain through reflective face c
+// (Omega.n < 0 with the face's own dot products): the first direction of the
+// set within 1e-14 (Euclidean) of Omega - 2 (Omega.n) n, n the unit
+// face-centre normal.  refl = -1 when there is none, -2 for angles that do not
+// enter through the face.
+__global__ void k_reflect(int nrefl, int Nw, int dim, const int* __restrict__ faces, const double* __restrict__ omega,
+                          const double* __restrict__ normals, const double* __restrict__ dots, int* __restrict__ refl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nrefl * Nw) return;
+    const int c = t / Nw, a = t % Nw;
+    const int f = faces[c];
+    if (!(dots[(size_t)f * Nw + a] < 0.0)) { refl[t] = -2; return; }
+    const double* n = normals + (size_t)f * dim;
+    double r[3] = {0, 0, 0};
+    double dn = 0.0;
+    for (int d = 0; d < dim; ++d) dn = __dadd_rn(dn, __dmul_rn(omega[a * dim + d], n[d]));
+    for (int d = 0; d < dim; ++d) r[d] = __dsub_rn(omega[a * dim + d], __dmul_rn(2.0 * dn, n[d]));
+    int found = -1;
+    for (int b = 0; b < Nw && found < 0; ++b) {
+        double d2 = 0.0;
+        for (int d = 0; d < dim; ++d) { const double x = omega[b * dim + d] - r[d]; d2 += x * x; }
+        if (sqrt(d2) < 1e-14) found = b;
+    }
+    refl[t] = found;
+}
+
+// Reflective edges (sweep.cpp:177-195) as two tables over [nrefl][Nw]:
+// d_refl[c][a] = reflected angle feeding entering angle a (else negative),
+// d_feed[c][b] = the entering angle that angle b feeds (else -1).
+int compute_reflections(Handle& h, const std::vector<int>& refl_faces) {
+    h.nrefl = (int)refl_faces.size();
+    if (h.nrefl == 0) return ALLIUM_OK;
+    const size_t total = (size_t)h.nrefl * h.Nw;
+    int* d_faces = nullptr;
+    cudaError_t e = cudaMalloc(&d_faces, refl_faces.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h.d_refl, total * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h.d_feed, total * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_faces, refl_faces.data(), refl_faces.size() * sizeof(int), cudaMemcpyHostToDevice, h.stream);
+    if (e == cudaSuccess) {
+        k_reflect<<<(int)((total + 127) / 128), 128, 0, h.stream>>>(h.nrefl, h.Nw, h.dim, d_faces, h.d_omega, h.d_normals,
+                                                                   h.d_dots, h.d_refl);
+        e = cudaGetLastError();
+    }
+    std::vector<int> refl(total), feed(total, -1);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(refl.data(), h.d_refl, total * sizeof(int), cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    if (d_faces) cudaFree(d_faces);
+    if (e != cudaSuccess) { h.last_error = cudaGetErrorString(e); return ALLIUM_ERR_CUDA; }
+    for (int c = 0; c < h.nrefl; ++c)
+        for (int a = 0; a < h.Nw; ++a) {
+            const int b = refl[(size_t)c * h.Nw + a];
+            if (b == -1) { h.last_error = "a reflected direction is not in the angular quadrature"; return ALLIUM_ERR_MESH; }
+            if (b < 0) continue;
+            int& slot = feed[(size_t)c * h.Nw + b];
+            if (slot >= 0) { h.last_error = "two directions reflect onto one"; return ALLIUM_ERR_MESH; }
+            slot = a;
+        }
+    e = cudaMemcpyAsync(h.d_feed, feed.data(), total * sizeof(int), cudaMemcpyHostToDevice, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    if (e != cudaSuccess) { h.last_error = cudaGetErrorString(e); return ALLIUM_ERR_CUDA; }
+    return ALLIUM_OK;
+}
+
 // ------------------------------------------------------------ assembly
 // One block per cell.  Geometric factors of each quadrature point are staged
 // in shared memory, then the threads share out the matrix entries.
@@ -314,6 +379,8 @@ __global__ void k_indegree(int ne, int Nw, int dim, const double* __restrict__ d
     int c = 0;
     for (int k = 0; k < nface; ++k) {
         const Slot s = slots[(size_t)e * nface + k];
+        // reflective face: edge (e, reflected a) -> (e, a) when Omega_a . n < 0 (sweep.cpp:181-194)
+        if (s.nbr <= -2) { if (dots[(size_t)s.face * Nw + a] < 0.0) ++c; continue; }
         if (s.nbr < 0) continue;
         const bool fwd = forward_edge(dots, Nw, s.face, a);
         if (s.side ? fwd : !fwd) ++c;
@@ -326,15 +393,26 @@ __global__ void k_indegree(int ne, int Nw, int dim, const double* __restrict__ d
 }
 
 __global__ void k_kahn(int Nw, int dim, const double* __restrict__ dots,
-                       const Slot* __restrict__ slots, int* __restrict__ indeg, int* __restrict__ level,
-                       const int* __restrict__ cur, int ncur, int* __restrict__ next, int* __restrict__ ncount,
-                       int lev) {
+                       const Slot* __restrict__ slots, const int* __restrict__ feed, int* __restrict__ indeg,
+                       int* __restrict__ level, const int* __restrict__ cur, int ncur, int* __restrict__ next,
+                       int* __restrict__ ncount, int lev) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncur) return;
     const int u = cur[t];
     const int e = u / Nw, a = u % Nw, nface = 2 * dim;
     for (int k = 0; k < nface; ++k) {
         const Slot s = slots[(size_t)e * nface + k];
+        if (s.nbr <= -2) {
+            const int t2 = feed[(size_t)(-2 - s.nbr) * Nw + a];
+            if (t2 >= 0) {
+                const int v = e * Nw + t2;
+                if (atomicSub(&indeg[v], 1) == 1) {
+                    level[v] = lev + 1;
+                    next[atomicAdd(ncount, 1)] = v;
+                }
+            }
+            continue;
+        }
         if (s.nbr < 0) continue;
         const bool fwd = forward_edge(dots, Nw, s.face, a);
         if (!(s.side ? !fwd : fwd)) continue;   // not an out-edge of u
@@ -379,7 +457,7 @@ int compute_levels(Handle& h) {
     while (ncur > 0) {
         done += ncur;
         CK(cudaMemsetAsync(d_cnt + 1, 0, sizeof(int), h.stream));
-        k_kahn<<<(ncur + b - 1) / b, b, 0, h.stream>>>(h.Nw, h.dim, h.d_dots, h.d_slots, d_indeg,
+        k_kahn<<<(ncur + b - 1) / b, b, 0, h.stream>>>(h.Nw, h.dim, h.d_dots, h.d_slots, h.d_feed, d_indeg,
                                                         h.d_level, d_fa, ncur, d_fb, d_cnt + 1, lev);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&ncur, d_cnt + 1, sizeof(int), cudaMemcpyDeviceToHost, h.stream));

@@ -9,9 +9,9 @@ cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi) {
     a.omega = h.d_omega; a.dots = h.f_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
     a.Gm = h.f_G; a.M = h.f_M; a.Mt = h.f_Mt; a.F = h.f_F; a.sigma = h.f_sigma;
     a.tau = (float)h.tau; a.td = h.time_dependent ? 1 : 0;
-    a.src = src; a.psi = psi; a.status = h.d_status;
+    a.src = src; a.psi = psi; a.status = h.d_status; a.refl = h.d_refl;
     a.fix_kind = h.fix_kind; a.fix_min = (float)h.fix_min; a.fix_counts = h.d_fix_counts;
-    if (h.schedule == 1 && h.p <= 1 && !h.fix_kind) {
+    if (h.schedule == 1 && h.p <= 1 && !h.fix_kind && h.nrefl == 0) {
         cudaError_t e = prepare_flow(h);
         if (e != cudaSuccess) return e;
         return run_graph(h, 13, src, psi, [&](cudaStream_t st) { return flow_dispatch<2, float>(h, a, nullptr, st); });
@@ -35,12 +35,13 @@ cudaError_t sweep_levels_nodes(Handle& h, const SweepArgs<float>& args, cudaStre
 }
 
 cudaError_t launch_sweep_nodes_f32(Handle& h, const float* src, float* psi) {
+    if (h.nrefl) return cudaErrorNotSupported;   // node layout: inflow/vacuum boundaries only
     SweepArgs<float> a;
     a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
     a.omega = h.d_omega; a.dots = h.f_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
     a.Gm = h.f_G; a.M = h.f_M; a.Mt = h.f_Mt; a.F = h.f_F; a.sigma = h.f_sigma;
     a.tau = (float)h.tau; a.td = h.time_dependent ? 1 : 0;
-    a.src = src; a.psi = psi; a.status = h.d_status;
+    a.src = src; a.psi = psi; a.status = h.d_status; a.refl = h.d_refl;
     a.fix_kind = h.fix_kind; a.fix_min = (float)h.fix_min; a.fix_counts = h.d_fix_counts;
     if (h.schedule == 1) {
         cudaError_t e = prepare_flow(h);

@@ -49,7 +49,7 @@ cudaError_t ensure_factors(Handle& h) {
     a.omega = h.d_omega; a.dots = h.d_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
     a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
     a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
-    a.src = nullptr; a.psi = nullptr; a.status = h.d_status;
+    a.src = nullptr; a.psi = nullptr; a.status = h.d_status; a.refl = h.d_refl;
     a.fix_kind = 0; a.fix_min = 0.0; a.fix_counts = nullptr;
     cudaError_t e;
     switch (h.dim * 10 + h.p) {
@@ -68,11 +68,11 @@ cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
     a.omega = h.d_omega; a.dots = h.d_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
     a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
     a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
-    a.src = src; a.psi = psi; a.status = h.d_status;
+    a.src = src; a.psi = psi; a.status = h.d_status; a.refl = h.d_refl;
     a.fix_kind = h.fix_kind; a.fix_min = (double)h.fix_min; a.fix_counts = h.d_fix_counts;
     if (h.fix_kind)   // the fixup needs the local matrix: rebuild and factor, level by level
         return run_graph(h, 21, src, psi, [&](cudaStream_t st) { return sweep_dispatch<double, true>(h, a, st); });
-    const bool flow = h.schedule == 1 && h.p <= 1;
+    const bool flow = h.schedule == 1 && h.p <= 1 && h.nrefl == 0;
     if (flow) {
         cudaError_t e = prepare_flow(h);
         if (e != cudaSuccess) return e;

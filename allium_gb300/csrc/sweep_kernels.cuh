@@ -39,6 +39,7 @@ struct SweepArgs {
     const R* src;
     R* psi;
     int* status;
+    const int* refl;   // [nrefl][Nw] reflected angle at reflective face c (slots with nbr = -2 - c)
     // negative-flux fixup (src/fixup.cpp): 0 none, 1 zero, 2 zero and scale
     int fix_kind;
     R fix_min;
@@ -348,6 +349,26 @@ __device__ __forceinline__ void assemble_rhs(const SweepArgs<R>& s, int e, int a
                 const int fi = face_dof(D, P, k, ii);
                 b[fi] = fma_r(rd, acc, b[fi]);
             }
+        } else if (dots[k] < R(0) && nbrs[k] <= -2) {
+            // reflective face: the same cell's trace in the reflected direction
+            // (sweep.cpp:432-437), face block F(self, self)
+            const int ar = s.refl[(size_t)(-2 - nbrs[k]) * s.Nw + a];
+            const R* own = s.psi + psi_index(s.ndof, s.Nw, g, ar, (long long)e * N);
+            R u[NF];
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) u[jj] = load_upstream(own + face_dof(D, P, k, jj), CG);
+            const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
+            const R rd = -dots[k];
+#pragma unroll
+            for (int ii = 0; ii < NF; ++ii) {
+                R frow[NF];
+                load_block<NF>(F + ii * NF, frow);
+                R acc = R(0);
+#pragma unroll
+                for (int jj = 0; jj < NF; ++jj) acc = fma_r(frow[jj], u[jj], acc);
+                const int fi = face_dof(D, P, k, ii);
+                b[fi] = fma_r(rd, acc, b[fi]);
+            }
         }
     }
 }
@@ -489,6 +510,16 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
             R acc = R(0);
 #pragma unroll
             for (int jj = 0; jj < NF; ++jj) acc = fma_r(frow[jj], up[map[jj]], acc);
+            br = fma_r(-dk, acc, br);
+        }
+        if (dk < R(0) && q.nbr <= -2 && on) {
+            const int ar = s.refl[(size_t)(-2 - q.nbr) * s.Nw + a];
+            const R* own = s.psi + psi_index(s.ndof, s.Nw, g, ar, (long long)e * N);
+            R frow[NF];
+            load_block<NF>(F, frow);
+            R acc = R(0);
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) acc = fma_r(frow[jj], own[face_dof(D, P, k, jj)], acc);
             br = fma_r(-dk, acc, br);
         }
     });

@@ -155,4 +155,17 @@ int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string&
     return ALLIUM_OK;
 }
 
+void mark_reflective(Topology& t, int nface, const std::vector<int>& refl_attrs) {
+    t.refl_faces.clear();
+    if (refl_attrs.empty()) return;
+    for (size_t i = 0; i < t.slots.size(); ++i) {
+        Slot& sl = t.slots[i];
+        if (sl.nbr != -1) continue;
+        if (std::find(refl_attrs.begin(), refl_attrs.end(), sl.attr) == refl_attrs.end()) continue;
+        sl.nbr = -2 - (int)t.refl_faces.size();
+        t.refl_faces.push_back(sl.face);
+    }
+    (void)nface;
+}
+
 }  // namespace allium

@@ -49,7 +49,8 @@ class InverseAdvectionOperator:
 
     mesh: allium_gb300.mesh.Mesh; order: DG order (0..3, Gauss-Lobatto basis);
     quad: allium_gb300.quadrature.AngularQuadrature; sigma_t: [G, Ne] total cross
-    section per cell; lump: allium lumping bit mask; bc: {attribute: "inflow"}.
+    section per cell; lump: allium lumping bit mask; bc: {attribute: "inflow" |
+    "reflective"} (attributes not listed are inflow/vacuum).
     """
 
     def __init__(self, mesh, order, quad, sigma_t, lump=0, bc=None):

@@ -41,7 +41,7 @@ enum allium_status {
     ALLIUM_ERR_TIMEOUT = 4,      /* a bounded device wait gave up */
     ALLIUM_ERR_NAN = 5,          /* non-finite value detected */
     ALLIUM_ERR_CUDA = 6,         /* CUDA runtime error (message in last_error) */
-    ALLIUM_ERR_UNSUPPORTED = 7,  /* option not implemented (reflective, fixup, ...) */
+    ALLIUM_ERR_UNSUPPORTED = 7,  /* option not implemented (order, fixup kind, ...) */
     ALLIUM_ERR_MESH = 8,         /* non-conforming or malformed mesh */
     ALLIUM_ERR_SINGULAR = 9      /* zero pivot in a local solve (mfem::LinearSolve fails) */
 };
@@ -96,8 +96,11 @@ typedef struct {
  * builds the upwind graph, its device wavefront levels and assembles the local
  * matrices.  sigma_t is the piecewise-constant total cross section
  * [num_groups][num_elements] (a MultiGroupCoefficient sampled per cell).
- * bc may be NULL (all INFLOW).  Reflective boundaries return
- * ALLIUM_ERR_UNSUPPORTED. */
+ * bc may be NULL (all INFLOW).  On REFLECTIVE boundaries a direction entering
+ * the domain takes the trace of its mirror direction in the same cell
+ * (src/sweep.cpp:177-195, 432-437); the mirror must be in the quadrature set
+ * (else ALLIUM_ERR_MESH), and mirror loops that close a cycle give
+ * ALLIUM_ERR_NOT_DAG as in the reference. */
 int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe,
                         const allium_quad_desc* quad, int num_groups,
                         const double* sigma_t, const allium_bc_desc* bc,

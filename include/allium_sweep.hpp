@@ -43,6 +43,13 @@ struct Mesh {
     std::vector<int> boundary_attributes;      // [nbf]
 };
 
+// boundary attribute -> ALLIUM_BC_INFLOW / ALLIUM_BC_REFLECTIVE (BoundaryConditionMap)
+struct BoundaryConditions {
+    std::vector<int> attributes;
+    std::vector<int> kinds;
+    void Set(int attribute, int kind) { attributes.push_back(attribute); kinds.push_back(kind); }
+};
+
 struct Quadrature {
     int dim = 0;
     std::vector<double> omega;    // [Nw][dim]
@@ -54,7 +61,8 @@ class InverseAdvectionOperator {
 public:
     // sigma_t: [G][Ne] piecewise-constant total cross section; lump: allium bit mask
     InverseAdvectionOperator(const Mesh& mesh, int order, const Quadrature& quad, int num_groups,
-                             const std::vector<double>& sigma_t, int lump = 0) {
+                             const std::vector<double>& sigma_t, int lump = 0,
+                             const BoundaryConditions& bc = BoundaryConditions()) {
         allium_mesh_desc m;
         m.dim = mesh.dim;
         m.num_vertices = (int)(mesh.vertices.size() / mesh.dim);
@@ -66,7 +74,8 @@ public:
         m.boundary_attributes = mesh.boundary_attributes.data();
         allium_fe_desc fe{order, ALLIUM_BASIS_GAUSS_LOBATTO, lump};
         allium_quad_desc q{quad.dim, quad.Size(), quad.omega.data(), quad.weights.data()};
-        check(allium_sweep_create(&m, &fe, &q, num_groups, sigma_t.data(), nullptr, &h_));
+        allium_bc_desc b{(int)bc.attributes.size(), bc.attributes.data(), bc.kinds.data()};
+        check(allium_sweep_create(&m, &fe, &q, num_groups, sigma_t.data(), bc.attributes.empty() ? nullptr : &b, &h_));
         long long n = 0;
         int nl = 0;
         check(allium_sweep_sizes(h_, &n, &ndof_, &nl), h_);

@@ -42,6 +42,7 @@ def lib():
         L.oracle_moments_transpose.argtypes = [vp, dp, dp, C.c_int, C.c_double, C.c_int]
         L.oracle_form_source.argtypes = [vp, dp, FN, dp, C.c_int, FN, dp]
         L.oracle_set_fixup.argtypes = [vp, C.c_int, C.c_double]
+        L.oracle_set_reflective.argtypes = [vp, C.c_int, ip]
         L.oracle_fixup_counts.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.oracle_scattering_source.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_l2_error.argtypes = [vp, dp, C.c_int, C.c_int, FN]
@@ -99,6 +100,12 @@ class OracleSweep:
 
     def set_time_absorption(self, tau):
         lib().oracle_set_time_absorption(self.h, float(tau))
+
+    def set_reflective(self, attributes):
+        """Mark boundary attributes reflective (BoundaryCondition::REFLECTIVE)."""
+        a = np.ascontiguousarray(list(attributes), dtype=np.int32)
+        if lib().oracle_set_reflective(self.h, int(a.size), _ip(a)) != 0:
+            raise ValueError("a reflected direction is not in the angular quadrature")
 
     def set_fixup(self, kind, minimum=0.0):
         lib().oracle_set_fixup(self.h, int(kind), float(minimum))

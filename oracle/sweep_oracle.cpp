@@ -142,6 +142,7 @@ struct Face {
     int attr;
     double nrm[3];        // unit normal at the face centre, out of e1
     int sb[2], sc[2][2];  // e2 face coords s = sb + sc * t (t = e1 face coords)
+    std::vector<int> refl;  // reflective boundary: reflected angle of each entering angle, else -1
 };
 
 struct Oracle {
@@ -158,6 +159,7 @@ struct Oracle {
     std::vector<double> basis_nodes;
     std::vector<double> Ms, Gm, Mt, F;  // see assemble()
     std::vector<int> indeg0;            // in-degree per node
+    std::vector<std::pair<int, int>> rout;  // reflective edges (from node, to node), sorted
     long long ndof() const { return (long long)ne * n; }
     long long psi_size() const { return (long long)G * Nw * ndof(); }
 };
@@ -462,6 +464,25 @@ void build_graph(Oracle& o) {
             }
             o.indeg0[(size_t)e * o.Nw + a] = c;
         }
+    // reflective boundary faces, sweep.cpp:177-195: for every angle entering
+    // the domain, an edge (e, reflected angle) -> (e, angle)
+    o.rout.clear();
+    for (const Face& f : o.faces) {
+        if (f.e2 >= 0 || f.refl.empty()) continue;
+        for (int a = 0; a < o.Nw; ++a) {
+            if (f.refl[a] < 0) continue;
+            o.indeg0[(size_t)f.e1 * o.Nw + a] += 1;
+            o.rout.emplace_back(f.e1 * o.Nw + f.refl[a], f.e1 * o.Nw + a);
+        }
+    }
+    std::sort(o.rout.begin(), o.rout.end());
+}
+
+// nodes fed by u through reflective faces
+template <class Fn>
+void for_reflective_out(const Oracle& o, int u, Fn&& fn) {
+    auto lo = std::lower_bound(o.rout.begin(), o.rout.end(), std::make_pair(u, -1));
+    for (; lo != o.rout.end() && lo->first == u; ++lo) fn(lo->second);
 }
 
 // mfem::LUFactors::Factor + Solve restated (partial pivoting, column major)
@@ -547,6 +568,18 @@ bool solve_node(const Oracle& o, int e, int a, const double* src, double* psi,
         for (int k = 0; k < nd; ++k) {
             const int fid = o.efaces[(size_t)e * nd + k];
             const Face& f = o.faces[fid];
+            if (f.e2 < 0 && !f.refl.empty() && f.refl[a] >= 0) {
+                // reflection, sweep.cpp:432-437: the same cell's values in the
+                // reflected angle through the face block (1,1)
+                const double dot = dotv(dim, Om, f.nrm);
+                const double* Fm = &o.F[((size_t)fid * 4) * nn];
+                for (int i = 0; i < n; ++i) {
+                    double s = 0.0;
+                    for (int j = 0; j < n; ++j) s += Fm[i * n + j] * psi[pidx(o, g, f.refl[a], off + j)];
+                    rhs[i] += -dot * s;
+                }
+                continue;
+            }
             if (!is_in_edge(o, e, f, a)) continue;
             const bool keep = (e == f.e1);
             double nor[3];
@@ -636,6 +669,36 @@ void oracle_set_time_absorption(void* h, double tau) {
     if (o.Mt.empty()) assemble_time_mass(o);
 }
 
+// Reflective boundary attributes (BoundaryCondition::REFLECTIVE).  The
+// reflected angle is GetReflectedAngleIndex (angular_quadrature.cpp:27-36):
+// the first direction within 1e-14 of Omega - 2 (Omega.n) n.  Returns 0, or
+// -1 when an entering direction has no reflection in the set.
+int oracle_set_reflective(void* h, int num, const int* attrs) {
+    Oracle& o = *static_cast<Oracle*>(h);
+    const int dim = o.dim;
+    int status = 0;
+    for (Face& f : o.faces) {
+        f.refl.clear();
+        if (f.e2 >= 0 || std::find(attrs, attrs + num, f.attr) == attrs + num) continue;
+        f.refl.assign(o.Nw, -1);
+        for (int a = 0; a < o.Nw; ++a) {
+            const double* Om = &o.omega[(size_t)a * dim];
+            const double dot = dotv(dim, Om, f.nrm);
+            if (!(dot < 0)) continue;
+            double r[3];
+            for (int d = 0; d < dim; ++d) r[d] = Om[d] - (2 * dot) * f.nrm[d];
+            for (int b = 0; b < o.Nw; ++b) {
+                double diff = 0.0;
+                for (int d = 0; d < dim; ++d) diff += std::pow(o.omega[(size_t)b * dim + d] - r[d], 2);
+                if (std::sqrt(diff) < 1e-14) { f.refl[a] = b; break; }
+            }
+            if (f.refl[a] < 0) status = -1;
+        }
+    }
+    build_graph(o);
+    return status;
+}
+
 void oracle_set_fixup(void* h, int kind, double minimum) {
     Oracle& o = *static_cast<Oracle*>(h);
     o.fix_kind = kind; o.fix_min = minimum; o.fix_applied = o.fix_failed = 0;
@@ -701,6 +764,9 @@ int oracle_levels(void* h, int* level) {
                 const int v = nbr * o.Nw + a;
                 if (--deg[v] == 0) { next.push_back(v); level[v] = lev + 1; }
             }
+            for_reflective_out(o, u, [&](int v) {
+                if (--deg[v] == 0) { next.push_back(v); level[v] = lev + 1; }
+            });
         }
         std::swap(cur, next);
         ++lev;
@@ -750,6 +816,9 @@ int oracle_sweep(void* h, const double* src, double* psi, int nthreads) {
                         const int v = nbr * o.Nw + a;
                         if (--deg[v] == 0) local.push_back(v);
                     }
+                    for_reflective_out(o, u, [&](int v) {
+                        if (--deg[v] == 0) local.push_back(v);
+                    });
                 }
             }
         }

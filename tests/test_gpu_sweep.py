@@ -367,9 +367,6 @@ def test_fixup_parity(dim, cells, kind):
 
 def test_errors_are_reported():
     mesh, quad, sig = problem(2, (4, 4), 1)
-    with pytest.raises(AlliumError) as e:
-        InverseAdvectionOperator(mesh, 1, quad, sig, bc={1: "reflective"})
-    assert e.value.status == 7
     m3, q3, s3 = problem(3, (2, 2, 2), 3)
     with pytest.raises(AlliumError) as e:
         InverseAdvectionOperator(m3, 3, q3, s3)
@@ -381,3 +378,102 @@ def test_errors_are_reported():
     assert e.value.status == 1
     with pytest.raises(ValueError):
         L.Mult(np.zeros(3), np.zeros(3))
+
+
+# --------------------------------------------------------------- reflective boundaries
+REFL_CASES = [
+    # dim, cells, p, S_N, G, reflective attributes
+    (1, (12,), 1, 4, 2, (2,)),
+    (2, (9, 7), 0, 4, 2, (2,)),
+    (2, (9, 7), 1, 6, 2, (2, 3)),
+    (2, (8, 6), 2, 4, 1, (1, 2)),
+    (2, (6, 5), 3, 4, 1, (3,)),
+    (3, (5, 4, 3), 1, 4, 2, (3, 4, 6)),
+    (3, (6, 6, 6), 1, 12, 1, (1, 2, 5)),
+    (3, (4, 3, 3), 2, 4, 1, (3,)),
+]
+
+
+@pytest.mark.parametrize("case", REFL_CASES, ids=[f"d{c[0]}p{c[2]}S{c[3]}r{''.join(map(str, c[5]))}" for c in REFL_CASES])
+def test_reflective_parity(case):
+    # reflective edges (sweep.cpp:177-195) and the reflected-angle face term
+    # (sweep.cpp:432-437) against the oracle: levels exact, FP64 to 1e-12
+    dim, cells, p, sn, G, attrs = case
+    mesh, quad, sig = problem(dim, cells, p, sn=sn, G=G, seed=13)
+    o = OracleSweep(mesh, p, quad, sig)
+    o.set_reflective(attrs)
+    L = InverseAdvectionOperator(mesh, p, quad, sig, bc={a: "reflective" for a in attrs})
+    nl, lev = o.levels()
+    assert L.num_levels == nl and np.array_equal(L.levels(), lev)
+    src = np.random.default_rng(3).random(o.psi_size)
+    ref = o.mult(src)
+    psi = np.empty_like(src)
+    L.Mult(src, psi)
+    assert rel_err(psi, ref) < TOL64
+    d = torch.from_numpy(src).cuda()
+    L.Mult(d, d)
+    f = torch.from_numpy(src.astype(np.float32)).cuda()
+    L.MultF32(f, f)
+    L.synchronize()
+    assert np.array_equal(d.cpu().numpy(), psi)
+    assert rel_err(f.cpu().numpy(), ref) < TOL32
+    if p == 1:
+        L.SetFactorCache(1)
+        L.Mult(d.copy_(torch.from_numpy(src)), d)
+        L.Mult(torch.from_numpy(src).cuda(), d)
+        L.synchronize()
+        assert rel_err(d.cpu().numpy(), ref) < TOL64
+        with pytest.raises(AlliumError) as e:
+            fn = torch.empty(o.psi_size, dtype=torch.float32, device="cuda")
+            L.MultF32Nodes(fn, fn)
+        assert e.value.status == 7
+    # the forward operator and the balance ignore the reflective coupling, as
+    # AdvectionOperator::Mult / ComputeBalance do (sweep.cpp:1246-1462)
+    y = np.empty_like(src)
+    AdvectionOperator(L).Mult(src, y)
+    assert rel_err(y, o.apply_L(src)) < TOL64
+    assert abs(AdvectionOperator(L).ComputeBalance(ref) - o.balance(ref)) < TOL64 * abs(o.balance(ref))
+
+
+def test_reflective_mirror_3d():
+    # 16 x 8 x 8 symmetric box against its 8^3 half with a reflective x = 1 face
+    full = M.cartesian((16, 8, 8), extents=(2.0, 1.0, 1.0))
+    half = M.cartesian((8, 8, 8))
+    quad = Q.level_symmetric(8, 3)
+
+    def centres(m):
+        return m.vertices[m.elements].mean(axis=1)
+
+    def sig(m):
+        c = centres(m)
+        return (1.0 + 3.0 * np.abs(c[:, 0] - 1.0) + c[:, 1] ** 2 + c[:, 2])[None, :]
+
+    def q(m):
+        c = centres(m)
+        return (1.0 + c[:, 0] * (2.0 - c[:, 0]) + 0.5 * c[:, 1])[None, :]
+
+    Lf = InverseAdvectionOperator(full, 1, quad, sig(full))
+    Lh = InverseAdvectionOperator(half, 1, quad, sig(half), bc={3: "reflective"})
+    pf = np.empty(Lf.width)
+    ph = np.empty(Lh.width)
+    Lf.Mult(FormTransportSource(Lf, q(full)), pf)
+    Lh.Mult(FormTransportSource(Lh, q(half)), ph)
+    cf, ch = centres(full), centres(half)
+    match = np.array([np.argmin(np.linalg.norm(cf - c, axis=1)) for c in ch])
+    pf = pf.reshape(1, quad.size, full.num_elements, 8)[:, :, match, :]
+    ph = ph.reshape(1, quad.size, half.num_elements, 8)
+    assert np.max(np.abs(pf - ph)) <= 1e-12 * np.max(np.abs(pf))
+
+
+def test_reflective_errors():
+    quad = Q.level_symmetric(4, 2)
+    mesh = M.cartesian((3, 3))
+    c, s = math.cos(0.3), math.sin(0.3)
+    mesh.vertices[:] = mesh.vertices @ np.array([[c, s], [-s, c]])
+    with pytest.raises(AlliumError) as e:
+        InverseAdvectionOperator(mesh, 1, quad, np.ones((1, 9)), bc={2: "reflective"})
+    assert e.value.status == 8
+    mesh, quad, sig = problem(2, (4, 3), 1)
+    with pytest.raises(AlliumError) as e:
+        InverseAdvectionOperator(mesh, 1, quad, sig, bc={2: "reflective", 4: "reflective"})
+    assert e.value.status == 2

@@ -168,3 +168,109 @@ def test_in_place_and_threads():
     b = x.copy()
     o.mult(b, b, threads=4)
     assert np.array_equal(a, b)
+
+
+# --------------------------------------------------------------- reflective boundaries
+def _centres(mesh):
+    v = mesh.vertices[mesh.elements]          # [ne][2^dim][dim]
+    return v.mean(axis=1)
+
+
+def _mirror_problem(dim, n, p, sn=4, G=2):
+    """Full box [0,2] x [0,1]^(dim-1) and its half [0,1]^dim with the x = 1 face
+    reflective; source and cross sections symmetric about x = 1."""
+    full = M.cartesian((2 * n,) + (n,) * (dim - 1), extents=(2.0,) + (1.0,) * (dim - 1))
+    half = M.cartesian((n,) * dim)
+    quad = Q.level_symmetric(sn, dim)
+
+    def sig(mesh):
+        c = _centres(mesh)
+        s = 1.0 + 3.0 * np.abs(c[:, 0] - 1.0) + c[:, 1] ** 2 + (c[:, 2] if dim == 3 else 0.0)
+        return np.stack([s * (g + 1) for g in range(G)])
+
+    def qfn(x, om, g):
+        return 1.0 + x[0] * (2.0 - x[0]) + 0.5 * x[1] + (0.25 * x[2] if dim == 3 else 0.0) + g
+
+    refl_attr = 2 if dim == 2 else 3          # x = max face
+    return full, half, quad, sig, qfn, refl_attr
+
+
+@pytest.mark.parametrize("dim,n,p", [(2, 4, 1), (2, 3, 2), (3, 3, 1)])
+def test_reflective_half_domain_equals_full_domain(dim, n, p):
+    # a reflective face is a mirror (sweep.cpp:177-195, 432-437): the half domain
+    # with reflection reproduces the symmetric full-domain solution cell by cell
+    full, half, quad, sig, qfn, attr = _mirror_problem(dim, n, p)
+    of = OracleSweep(full, p, quad, sig(full))
+    oh = OracleSweep(half, p, quad, sig(half))
+    oh.set_reflective([attr])
+    pf = of.mult(of.form_source(qfn=qfn))
+    ph = oh.mult(oh.form_source(qfn=qfn))
+    cf, ch = _centres(full), _centres(half)
+    match = np.array([np.argmin(np.linalg.norm(cf - c, axis=1)) for c in ch])
+    n_loc = (p + 1) ** dim
+    pf = pf.reshape(of.G, of.Nw, full.num_elements, n_loc)[:, :, match, :]
+    ph = ph.reshape(oh.G, oh.Nw, half.num_elements, n_loc)
+    assert np.max(np.abs(pf - ph)) <= 1e-12 * np.max(np.abs(pf))
+    # the reflective face adds in-edges: more levels than the vacuum half domain
+    assert oh.levels()[0] > OracleSweep(half, p, quad, sig(half)).levels()[0]
+
+
+def _reflect_mms(ne, p):
+    # test/chive/mms.lua without scattering: [0, 0.5] x [0, 1], reflective at x = 0.5
+    alpha, beta, delta, total = 0.25, 0.5, 2.0, 1.0
+    pi = math.pi
+
+    def psi(x, om, g):
+        mu, eta = om[0], om[1]
+        return (math.sin(pi * x[0]) * math.sin(pi * x[1])
+                + beta * (mu + eta) * math.sin(2 * pi * x[0]) * math.sin(2 * pi * x[1])
+                + alpha * (mu * mu + eta * eta) * math.sin(3 * pi * x[0]) * math.sin(3 * pi * x[1]) + delta) / 4 / pi
+
+    def q(x, om, g):
+        mu, eta = om[0], om[1]
+        dx = (math.cos(pi * x[0]) * math.sin(pi * x[1]) / 4
+              + beta * (mu + eta) * math.cos(2 * pi * x[0]) * math.sin(2 * pi * x[1]) / 2
+              + alpha * (mu * mu + eta * eta) * math.cos(3 * pi * x[0]) * math.sin(3 * pi * x[1]) * 3 / 4)
+        dy = (math.sin(pi * x[0]) * math.cos(pi * x[1]) / 4
+              + beta * (mu + eta) * math.sin(2 * pi * x[0]) * math.cos(2 * pi * x[1]) / 2
+              + alpha * (mu * mu + eta * eta) * math.sin(3 * pi * x[0]) * math.cos(3 * pi * x[1]) * 3 / 4)
+        return mu * dx + eta * dy + total * psi(x, om, g)
+
+    mesh = M.cartesian((ne // 2, ne), extents=(0.5, 1.0))
+    quad = Q.level_symmetric(4, 2)
+    o = OracleSweep(mesh, p, quad, np.full((1, mesh.num_elements), total))
+    o.set_reflective([2])
+    # inflow on every boundary face; on the reflective face the manufactured
+    # solution is mirror symmetric, so the exact trace is the reflected one
+    src = o.form_source(qfn=q, inflow_fn=lambda x, om, g, a: 0.0 if a == 2 else psi(x, om, g))
+    sol = o.mult(src)
+    return max(o.l2_error(sol, 0, a, psi) for a in range(quad.size))
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_reflective_mms_order(p):
+    # test/chive/mms.lua + test_ooa.py: L2 order p + 1 +- 0.2 with a reflective side
+    e1 = _reflect_mms(10, p)
+    e2 = _reflect_mms(20, p)
+    assert abs(math.log2(e1 / e2) - (p + 1)) < 0.2
+
+
+def test_reflective_errors():
+    # a rotated box: the mirror images of S4 directions are not in the set
+    mesh = M.cartesian((3, 3))
+    c, s = math.cos(0.3), math.sin(0.3)
+    mesh.vertices[:] = mesh.vertices @ np.array([[c, s], [-s, c]])
+    quad = Q.level_symmetric(4, 2)
+    o = OracleSweep(mesh, 1, quad, np.ones((1, 9)))
+    with pytest.raises(ValueError):
+        o.set_reflective([2])
+    # two opposite reflective sides close a cycle, which the reference rejects
+    mesh, quad, sigma = problem(2, (4, 3), 1)
+    o = OracleSweep(mesh, 1, quad, sigma)
+    o.set_reflective([2, 4])
+    assert o.levels()[0] == -1
+    with pytest.raises(RuntimeError):
+        o.mult(np.ones(o.psi_size))
+    # adjacent reflective sides (a symmetric quarter) stay a DAG
+    o.set_reflective([2, 3])
+    assert o.levels()[0] > 0
