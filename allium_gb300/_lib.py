@@ -65,6 +65,17 @@ EXPORTS = {
     "allium_sweep_moments_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_levels": (C.c_int, [C.c_void_p, C.c_void_p]),
     "allium_sweep_selftest_wait": (C.c_int, [C.c_void_p, C.c_int]),
+    "allium_planck_spectrum": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_void_p]),
+    "allium_sweep_planck_emission": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                               C.c_void_p]),
+    "allium_sweep_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                              C.c_void_p, C.c_void_p]),
+    "allium_sweep_block_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double,
+                                           C.c_int]),
+    "allium_sweep_absorption": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int]),
+    "allium_sweep_time_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "allium_sweep_powerlaw_opacity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                                C.c_void_p]),
     "allium_sweep_synchronize": (C.c_int, [C.c_void_p]),
     "allium_sweep_last_error": (C.c_char_p, [C.c_void_p]),
     "allium_status_string": (C.c_char_p, [C.c_int]),

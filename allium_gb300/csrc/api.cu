@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "planck.cuh"
 
 using allium::Handle;
 
@@ -66,7 +67,7 @@ void free_all(Handle& h) {
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
                     h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts,
-                    h.d_refl, h.d_feed};
+                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -613,6 +614,111 @@ int allium_sweep_fixup_counts(allium_sweep* s, long long* applied, long long* fa
     }
     if (applied) *applied = (long long)c[0];
     if (failed) *failed = (long long)c[1];
+    return ALLIUM_OK;
+}
+
+// ------------------------------------------------------------ thermal radiative transfer
+int allium_planck_spectrum(const double* bounds, int num_groups, double T, int kind, double* out) {
+    if (!bounds || !out || num_groups < 1 || (kind != 0 && kind != 1) || !(T > 0.0)) return ALLIUM_ERR_ARG;
+    double prev = 0.0;
+    for (int g = 0; g < num_groups - 1; ++g) {
+        const double x = bounds[g + 1] / T;
+        double f = allium::planck_fraction(x);
+        if (kind == 1) f = allium::rosseland_from_planck(x, f);
+        out[g] = f - prev;
+        prev = f;
+    }
+    out[num_groups - 1] = 1.0 - prev;
+    return ALLIUM_OK;
+}
+
+static int trt_check(Handle& h, const char* who) {
+    if (!allium::trt_supported(h)) {
+        h.last_error = std::string(who) + ": at most 16 DOFs per cell and no lumping";
+        return ALLIUM_ERR_UNSUPPORTED;
+    }
+    return ALLIUM_OK;
+}
+
+int allium_sweep_planck_emission(allium_sweep* s, const double* bounds, const double* sigma_abs, const double* T,
+                                 double ac, double* emission, double* grad) {
+    if (!s || !bounds || !sigma_abs || !T || (!emission && !grad)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = trt_check(h, "allium_sweep_planck_emission")) return st;
+    if (int st = device_only(h, {sigma_abs, T}, "allium_sweep_planck_emission")) return st;
+    if ((emission && !on_device(emission)) || (grad && !on_device(grad))) {
+        h.last_error = "allium_sweep_planck_emission: outputs must be device memory";
+        return ALLIUM_ERR_ARG;
+    }
+    if (int st = upload(h, bounds, (size_t)h.G + 1, &h.d_bounds)) return st;
+    CUDA_OR_FAIL(h, allium::launch_trt_emission(h, h.d_bounds, sigma_abs, T, ac, 0.0, emission, grad, nullptr, nullptr));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_energy_balance(allium_sweep* s, const double* bounds, const double* sigma_abs, const double* T,
+                                double ac, double cv_dt, double* residual, double* grad_inv) {
+    if (!s || !bounds || !sigma_abs || !T || (!residual && !grad_inv)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = trt_check(h, "allium_sweep_energy_balance")) return st;
+    if (int st = device_only(h, {sigma_abs, T}, "allium_sweep_energy_balance")) return st;
+    if ((residual && !on_device(residual)) || (grad_inv && !on_device(grad_inv))) {
+        h.last_error = "allium_sweep_energy_balance: outputs must be device memory";
+        return ALLIUM_ERR_ARG;
+    }
+    if (int st = upload(h, bounds, (size_t)h.G + 1, &h.d_bounds)) return st;
+    if (int st = ensure_mass2(h)) return st;
+    CUDA_OR_FAIL(h, allium::launch_trt_emission(h, h.d_bounds, sigma_abs, T, ac, cv_dt, nullptr, nullptr, residual,
+                                                grad_inv));
+    if (grad_inv) return check_status(h);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_block_apply(allium_sweep* s, const double* blocks, int num_sets, const double* x, int x_shared,
+                             double* y, double alpha, int accumulate) {
+    if (!s || !x || !y || num_sets < 1) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    const double* B = blocks;
+    if (!blocks) {
+        // the handle's own mass matrices: num_sets 1 -> unit sigma mass, 2 -> MassIntegrator mass
+        if (num_sets == 2) {
+            if (int st = ensure_mass2(h)) return st;
+            B = h.d_Mt;
+        } else {
+            B = h.d_M;
+        }
+        num_sets = 1;
+    }
+    if (int st = device_only(h, {B, x, y}, "allium_sweep_block_apply")) return st;
+    CUDA_OR_FAIL(h, allium::launch_block_apply(h, B, num_sets, x, x_shared ? 0 : h.ndof, y, alpha, accumulate));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_absorption(allium_sweep* s, const double* sigma_abs, const double* phi, double* y, double alpha,
+                            int accumulate) {
+    if (!s || !sigma_abs || !phi || !y) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {sigma_abs, phi, y}, "allium_sweep_absorption")) return st;
+    CUDA_OR_FAIL(h, allium::launch_absorption(h, sigma_abs, phi, y, alpha, accumulate));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_time_source(allium_sweep* s, const double* psi_prev, const double* q, double tau, double* out) {
+    if (!s || !psi_prev || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {psi_prev, out}, "allium_sweep_time_source")) return st;
+    if (q && !on_device(q)) { h.last_error = "allium_sweep_time_source: q must be device memory"; return ALLIUM_ERR_ARG; }
+    if (int st = ensure_mass2(h)) return st;
+    CUDA_OR_FAIL(h, allium::launch_time_source(h, psi_prev, q, tau, out));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_powerlaw_opacity(allium_sweep* s, const double* T, const double* nu, double C, double a, double b,
+                                  double* sigma_out) {
+    if (!s || !T || !nu || !sigma_out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {T, sigma_out}, "allium_sweep_powerlaw_opacity")) return st;
+    if (int st = upload(h, nu, (size_t)h.G, &h.d_nu)) return st;
+    CUDA_OR_FAIL(h, allium::launch_powerlaw_opacity(h, T, h.d_nu, C, a, b, sigma_out));
     return ALLIUM_OK;
 }
 

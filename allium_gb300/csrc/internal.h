@@ -20,9 +20,10 @@ struct RefTables {
     int dim, p, n1, n, nf, nface;
     double nodes[kMaxOrder + 1];          // Gauss-Lobatto basis nodes on [0,1]
     // 1D rules: 0 = sigma mass, 1 = convection, 2 = time mass, 3 = face mass,
-    //           4 = source domain, 5 = source boundary
-    int rn[6];
-    double rx[6][kMaxRule], rw[6][kMaxRule];
+    //           4 = source domain, 5 = source boundary, 6 = Planck emission
+    //           (order 2p + 1), 7 = gray emission (order 2p + 2)
+    int rn[8];
+    double rx[8][kMaxRule], rw[8][kMaxRule];
 };
 
 // Per (cell, local face) topology.  nbr >= 0: interior face; nbr = -1:
@@ -91,6 +92,10 @@ struct Handle {
     int nrefl = 0;
     int* d_refl = nullptr;           // [nrefl][Nw] reflected angle feeding each entering angle
     int* d_feed = nullptr;           // [nrefl][Nw] entering angle fed by each angle
+
+    // thermal radiative transfer inputs (group bounds, group midpoints)
+    double* d_bounds = nullptr;      // [G + 1]
+    double* d_nu = nullptr;          // [G]
 
     // negative-flux fixup
     int fix_kind = 0;
@@ -169,6 +174,17 @@ cudaError_t launch_face_normals(Handle& h);
 cudaError_t launch_face_dots(Handle& h);
 cudaError_t launch_assemble(Handle& h);
 int compute_reflections(Handle& h, const std::vector<int>& refl_faces);   // allium status
+
+// thermal radiative transfer operators (trt.cu)
+bool trt_supported(const Handle& h);
+cudaError_t launch_trt_emission(Handle& h, const double* bounds, const double* sigma, const double* T, double K,
+                                double cv_dt, double* emission, double* dB, double* bt, double* bt_inv);
+cudaError_t launch_block_apply(Handle& h, const double* B, int nb, const double* x, long long x_stride, double* y,
+                               double alpha, int accumulate);
+cudaError_t launch_absorption(Handle& h, const double* sigma, const double* phi, double* y, double alpha, int accumulate);
+cudaError_t launch_time_source(Handle& h, const double* psi_prev, const double* q, double tau, double* out);
+cudaError_t launch_powerlaw_opacity(Handle& h, const double* T, const double* nu, double C, double a, double b,
+                                    double* sigma);
 cudaError_t launch_time_mass(Handle& h);
 int compute_levels(Handle& h);   // returns an allium status
 cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out);

@@ -99,6 +99,9 @@ RefTables make_ref_tables(int dim, int p, int lump) {
     set_rule(t, 3, p + 1, lump & ALLIUM_LUMP_FACE);
     set_rule(t, 4, p + 1, false);
     set_rule(t, 5, hi, false);
+    // IntRules.Get(geom, 2p + 1) and (geom, 2p + 2): n = order / 2 + 1 points
+    set_rule(t, 6, p + 1, false);
+    set_rule(t, 7, p + 2, false);
     return t;
 }
 

@@ -198,11 +198,29 @@ def solve_gmres(op: SchurOperator, q, tol=1e-8, restart=30, maxiter=2000):
 def refine(op: SchurOperator, q, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=20, inner_maxiter=500):
     """FP32-inner / FP64-outer iterative refinement on T phi = b."""
     t0 = time.perf_counter()
-    b = op.rhs(q)
+    res = refine_rhs(op, op.rhs(q), tol=tol, inner_tol=inner_tol, restart=restart, max_outer=max_outer,
+                     inner_maxiter=inner_maxiter)
+    res.seconds = time.perf_counter() - t0
+    return res
+
+
+def refine_rhs(op, b, x0=None, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=20, inner_maxiter=500):
+    """Iterative refinement on T phi = b from phi = x0 (zero when None): the
+    residual with op.apply (FP64 sweep), corrections by GMRES on op.apply32."""
+    t0 = time.perf_counter()
     bnorm = torch.linalg.norm(b).item()
-    phi = torch.zeros_like(b)
-    r = b.clone()
+    if bnorm == 0.0:
+        res = SolveResult(torch.zeros_like(b), 0, True, [0.0], 0.0, op.sweeps64, op.sweeps32)
+        res.inner_iterations = 0
+        return res
     w = torch.empty_like(b)
+    if x0 is None:
+        phi = torch.zeros_like(b)
+        r = b.clone()
+    else:
+        phi = x0.clone()
+        op.apply(phi, w)
+        r = b - w
     hist = []
     conv = False
     outer = 0

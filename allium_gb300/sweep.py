@@ -162,8 +162,15 @@ class InverseAdvectionOperator:
         return psi
 
     def AssembleLocalMatrices(self, sigma_t=None):
+        """Reassemble with new total cross sections [G, Ne] (numpy, or a float64
+        CUDA tensor read in place on the device)."""
         if sigma_t is None:
             sigma_t = self._keep[6]
+        if torch is not None and isinstance(sigma_t, torch.Tensor) and sigma_t.is_cuda:
+            if sigma_t.dtype != torch.float64 or not sigma_t.is_contiguous() or sigma_t.numel() != self.G * self.mesh.num_elements:
+                raise ValueError("sigma_t must be a contiguous float64 tensor of G * Ne entries")
+            check(_lib.lib().allium_sweep_assemble(self.h, C.c_void_p(sigma_t.data_ptr())), self.h)
+            return
         sig = np.ascontiguousarray(sigma_t, dtype=np.float64).reshape(self.G, -1)
         self._keep[6] = sig
         check(_lib.lib().allium_sweep_assemble(self.h, C.c_void_p(sig.ctypes.data)), self.h)

@@ -198,6 +198,41 @@ def solve_section(L, mesh, quad, sigma, src, maxiter=400):
     return out
 
 
+def trt_section(steps):
+    """Multigroup Marshak wave (linearized TRT): 128 x 128 quads of [0,1]^2, p = 1,
+    S8, 32 log-spaced groups over [1e-2, 10], sigma_g = 10 nu_g^-3 T^-1/2 per cell
+    (explicit in each step), c_v = 1, a = c = 1, T0 = 1e-3, Planck inflow at T = 1
+    on x = 0, backward Euler dt = 1e-3; each step's Schur system solved to 1e-8
+    by FP64 GMRES and by FP32-inner / FP64-outer refinement, the same steps."""
+    import torch
+    from allium_gb300.trt import marshak_wave
+    out = {"problem": "multigroup Marshak wave, 128x128 quads, p=1, S8 (40 directions), 32 groups, dt=1e-3, "
+                      "tol 1e-8 per step, no DSA", "steps": steps}
+    T = {}
+    for method in ("fp64", "ir"):
+        s = marshak_wave(method=method)
+        torch.cuda.synchronize()
+        secs, its, s64, s32, conv = 0.0, [], 0, 0, True
+        for _ in range(steps):
+            r = s.step()
+            secs += r.seconds
+            its.append(r.iterations)
+            s64 += r.sweeps64
+            s32 += r.sweeps32
+            conv = conv and r.converged
+        T[method] = s.T.clone()
+        psi_entries = s.L.width
+        out[method] = {"seconds": secs, "ms_per_step": 1e3 * secs / steps, "krylov_iterations": int(np.sum(its)),
+                       "max_iterations": int(np.max(its)), "fp64_sweeps": s64, "fp32_sweeps": s32, "converged": conv,
+                       "T_max": float(s.T.max().item())}
+        del s
+        torch.cuda.empty_cache()
+    out["psi_entries"] = psi_entries
+    out["speedup"] = out["fp64"]["seconds"] / out["ir"]["seconds"]
+    out["T_rel_diff"] = float((torch.max(torch.abs(T["ir"] - T["fp64"])) / torch.max(torch.abs(T["fp64"]))).item())
+    return out
+
+
 def chive2d_section(cpu=True):
     """The 2D chive configuration: 64x64 quads, p = 1, S8, sigma_t = 1,
     sigma_s = 0.9, q = 1, vacuum; source iteration to 1e-8 relative change of
@@ -404,6 +439,7 @@ def run_gpu(args):
     if not args.no_solve:
         line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0])
         line["chive_2d"] = chive2d_section(cpu=not args.no_cpu)
+        line["trt_marshak"] = trt_section(args.trt_steps)
     if not args.no_cpu and tuple(cells) == CELLS:
         rates, size = cpu_sweep_sample(os.cpu_count() or 1, 3, 1)
         line["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": os.cpu_count(),
@@ -423,6 +459,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cells", type=int, default=CELLS[0], help="cells per axis (smaller cases for profiling)")
     ap.add_argument("--no-solve", action="store_true", help="skip the time-to-tolerance solves")
+    ap.add_argument("--trt-steps", type=int, default=200, help="time steps of the multigroup TRT section")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -242,6 +242,64 @@ int allium_sweep_levels(allium_sweep* s, int* levels);
  * ALLIUM_ERR_TIMEOUT with the device still usable. */
 int allium_sweep_selftest_wait(allium_sweep* s, int poll_limit);
 
+/* ---- thermal radiative transfer operators around the sweep ----
+ * The operators LinearizedTRTOperator::Mult (src/trt_linearized.cpp:230-312)
+ * applies between sweeps.  Temperature T is a DG field on the sweep's
+ * elements (Ndof entries, same local DOF order as psi); moment vectors are
+ * [G][Ndof] (the moment layout with one moment); sigma_abs is the absorption
+ * opacity [G][Ne], piecewise constant per cell (sigma_fe_order = 0); ac is the
+ * "StefanBoltzmann" constant of src/constants.hpp (a c).  Vectors are device
+ * memory; bounds[G + 1] and nu[G] may be host or device.  At most 16 DOFs per
+ * cell and no lumping (ALLIUM_ERR_UNSUPPORTED otherwise). */
+
+/* EvalPlanckSpectrum (kind 0) / EvalRosselandSpectrum (kind 1)
+ * (src/planck.hpp:157-236): group fractions of the normalised spectrum at
+ * temperature T; host arrays, no handle. */
+int allium_planck_spectrum(const double* bounds, int num_groups, double T, int kind, double* out);
+
+/* PlanckEmissionNonlinearForm::Mult and ::GetGradient with PlanckEmissionNFI
+ * (src/trt_integrators.cpp:56-152, 229-302): emission[g][i] =
+ * int sigma_g ac T^4 b_g(T) phi_i, grad[g][e][i][j] = int sigma_g 4 ac T^3
+ * r_g(T) phi_i phi_j (row major blocks).  Either output may be NULL. */
+int allium_sweep_planck_emission(allium_sweep* s, const double* bounds, const double* sigma_abs, const double* T,
+                                 double ac, double* emission, double* grad);
+
+/* The energy-balance form meb_form of exe/scallion.cpp:755-765
+ * (GrayPlanckEmissionNFI, src/trt_integrators.cpp:154-208, plus
+ * MassIntegrator(c_v/dt)): residual[i] = int sum_g sigma_g b_g ac T^4 phi_i +
+ * cv_dt (M T)_i and grad_inv[e] = the inverse of its gradient block
+ * (DenseBlockDiagonalSolver over DenseMatrixInverse).  A singular block gives
+ * ALLIUM_ERR_SINGULAR. */
+int allium_sweep_energy_balance(allium_sweep* s, const double* bounds, const double* sigma_abs, const double* T,
+                                double ac, double cv_dt, double* residual, double* grad_inv);
+
+/* Block-diagonal product y_b = alpha B_b x_b (+ y_b when accumulate) for
+ * num_sets block sets B[num_sets][Ne][n][n]; x_shared: x is one [Ndof] vector
+ * for every set (the gradient of the emission applied to a temperature).
+ * blocks == NULL uses the handle's mass matrices: num_sets 1 the unit sigma
+ * mass (MGMassIntegrator rule), 2 the MassIntegrator mass (time absorption,
+ * heat capacity). */
+int allium_sweep_block_apply(allium_sweep* s, const double* blocks, int num_sets, const double* x, int x_shared,
+                             double* y, double alpha, int accumulate);
+
+/* y = alpha sum_g M_{sigma_g} phi_g (+ y): Mtot_collapse of
+ * exe/scallion.cpp:786-797 (MGMassIntegrator(total) summed over groups). */
+int allium_sweep_absorption(allium_sweep* s, const double* sigma_abs, const double* phi, double* y, double alpha,
+                            int accumulate);
+
+/* out = q + tau M psi_prev per (group, angle, cell) block: SNTimeMassMatrix::Mult
+ * (src/tvector.cpp:76-95) and the backward-Euler source of
+ * exe/scallion.cpp:1358-1359 (tau = 1/(c dt)).  q may be NULL; out may alias
+ * psi_prev or q. */
+int allium_sweep_time_source(allium_sweep* s, const double* psi_prev, const double* q, double tau, double* out);
+
+/* sigma_out[g][e] = C nu_g^a T_c^b, T_c the temperature at the cell centre:
+ * an analytic opacity (src/opacity.cpp:47-63) at the group midpoints nu_g,
+ * projected onto piecewise constants (OpacityCoefficient::Project with
+ * sigma_fe_order = 0). */
+int allium_sweep_powerlaw_opacity(allium_sweep* s, const double* T, const double* nu, double C, double a, double b,
+                                  double* sigma_out);
+
 /* Wait for the handle's stream; report sticky kernel errors and clear them. */
 int allium_sweep_synchronize(allium_sweep* s);
 

@@ -43,6 +43,13 @@ def lib():
         L.oracle_form_source.argtypes = [vp, dp, FN, dp, C.c_int, FN, dp]
         L.oracle_set_fixup.argtypes = [vp, C.c_int, C.c_double]
         L.oracle_set_reflective.argtypes = [vp, C.c_int, ip]
+        L.oracle_planck_spectrum.argtypes = [dp, C.c_int, C.c_double, C.c_int, dp]
+        L.oracle_planck_emission.argtypes = [vp, dp, dp, dp, C.c_double, dp, dp]
+        L.oracle_energy_balance.argtypes = [vp, dp, dp, dp, C.c_double, C.c_double, dp, dp]
+        L.oracle_time_source.argtypes = [vp, dp, dp, C.c_double, dp]
+        L.oracle_mass_apply.argtypes = [vp, C.c_int, dp, dp]
+        L.oracle_absorption.argtypes = [vp, dp, dp, dp]
+        L.oracle_powerlaw_opacity.argtypes = [vp, dp, dp, C.c_double, C.c_double, C.c_double, dp]
         L.oracle_fixup_counts.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.oracle_scattering_source.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_l2_error.argtypes = [vp, dp, C.c_int, C.c_int, FN]
@@ -65,6 +72,14 @@ def _f64(a):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def planck_spectrum(bounds, T, kind=0):
+    """Group fractions of the normalised Planck (0) or Rosseland (1) spectrum."""
+    b = _f64(bounds)
+    out = np.empty(b.size - 1)
+    lib().oracle_planck_spectrum(_dp(b), b.size - 1, float(T), int(kind), _dp(out))
+    return out
 
 
 class OracleSweep:
@@ -100,6 +115,43 @@ class OracleSweep:
 
     def set_time_absorption(self, tau):
         lib().oracle_set_time_absorption(self.h, float(tau))
+
+    # --- thermal radiative transfer operators (src/planck.hpp, src/trt_integrators.cpp)
+    def planck_emission(self, bounds, sigma, T, ac=1.0):
+        em = np.empty(self.G * self.ndof)
+        grad = np.empty(self.G * self.ne * self.n * self.n)
+        lib().oracle_planck_emission(self.h, _dp(_f64(bounds)), _dp(_f64(sigma)), _dp(_f64(T)), float(ac),
+                                     _dp(em), _dp(grad))
+        return em, grad.reshape(self.G, self.ne, self.n, self.n)
+
+    def energy_balance(self, bounds, sigma, T, ac, cv_dt):
+        res = np.empty(self.ndof)
+        grad = np.empty(self.ne * self.n * self.n)
+        lib().oracle_energy_balance(self.h, _dp(_f64(bounds)), _dp(_f64(sigma)), _dp(_f64(T)), float(ac),
+                                    float(cv_dt), _dp(res), _dp(grad))
+        return res, grad.reshape(self.ne, self.n, self.n)
+
+    def time_source(self, psi_prev, q, tau):
+        out = np.empty(self.psi_size)
+        qq = _f64(q) if q is not None else None
+        lib().oracle_time_source(self.h, _dp(_f64(psi_prev)), _dp(qq) if qq is not None else None, float(tau),
+                                 _dp(out))
+        return out
+
+    def mass_apply(self, which, x):
+        y = np.empty(self.ndof)
+        lib().oracle_mass_apply(self.h, int(which), _dp(_f64(x)), _dp(y))
+        return y
+
+    def absorption(self, sigma, phi):
+        y = np.empty(self.ndof)
+        lib().oracle_absorption(self.h, _dp(_f64(sigma)), _dp(_f64(phi)), _dp(y))
+        return y
+
+    def powerlaw_opacity(self, T, nu, C0, a, b):
+        out = np.empty(self.G * self.ne)
+        lib().oracle_powerlaw_opacity(self.h, _dp(_f64(T)), _dp(_f64(nu)), float(C0), float(a), float(b), _dp(out))
+        return out.reshape(self.G, self.ne)
 
     def set_reflective(self, attributes):
         """Mark boundary attributes reflective (BoundaryCondition::REFLECTIVE)."""

@@ -22,6 +22,12 @@
 //   src/transport_op.cpp:3-89 DiscreteToMoment Mult / MultTranspose / AddMultTranspose
 //   src/tvector.hpp:47-70   RIGHT layout psi(g,a,i) = i + Ndof*(a + Nw*g),
 //                           moments phi(g,m,i) = i + Ndof*(g + G*m)
+//   src/sweep.cpp:177-195,432-437, src/angular_quadrature.cpp:8-36
+//                           reflective boundaries (mirror angle edges and trace)
+//   src/fixup.cpp:3-57      zero / zero-and-scale negative-flux fixups
+//   src/planck.hpp:157-236  Planck / Rosseland group integrals
+//   src/trt_integrators.cpp:56-302, exe/scallion.cpp:755-797,1352-1470,
+//   src/tvector.cpp:76-95   TRT emission, energy balance, absorption, time source
 // Third-party arithmetic the reference takes from MFEM (@171eeb40, not present
 // here) is restated from MFEM's published algorithms: L2 Gauss-Lobatto tensor
 // basis with lexicographic local DOFs, Gauss-Legendre rules with MFEM's point
@@ -1082,6 +1088,245 @@ double oracle_l2_error(void* h, const double* psi, int g, int ang, oracle_fn exa
         err += loc;
     }
     return std::sqrt(err);
+}
+
+
+// ---------------------------------------------------------------- thermal radiative transfer
+// Planck integrals (src/planck.hpp:157-236): b(x) = 15/pi^4 int_0^x t^3/(e^t - 1)
+// as min(Taylor through x^21, 9-term polylogarithm), the Rosseland form
+// r(x) = b(x) - 15/(4 pi^4) x^4/(e^x - 1), group fractions with F = 0 below the
+// first and F = 1 above the last group.  The Taylor coefficients come from
+// Bernoulli numbers generated here by their recurrence.
+static double oracle_bernoulli_coef(int n) {
+    static double c[19];
+    static bool ready = false;
+    if (!ready) {
+        double B[19];
+        B[0] = 1.0;
+        for (int m = 1; m <= 18; ++m) {
+            double s = 0.0, binom = 1.0;   // C(m+1, k)
+            for (int k = 0; k < m; ++k) {
+                s += binom * B[k];
+                binom = binom * (m + 1 - k) / (k + 1);
+            }
+            B[m] = -s / (m + 1);
+        }
+        double fact = 1.0;
+        for (int k = 0; k <= 18; ++k) {
+            if (k > 0) fact *= k;
+            c[k] = (k >= 3 && k % 2 == 1) ? 0.0 : B[k] / (fact * (k + 3));
+        }
+        ready = true;
+    }
+    return c[n];
+}
+
+static double oracle_planck_b(double x) {
+    const double pi = 3.14159265358979323846;
+    const double norm = 15.0 / (pi * pi * pi * pi);
+    if (x > 1e100) return 1.0;
+    if (x == 0.0) return 0.0;
+    double taylor = 0.0;
+    for (int k = 0; k <= 18; ++k) taylor += oracle_bernoulli_coef(k) * std::pow(x, k + 3);
+    taylor *= norm;
+    double poly = 0.0;
+    for (int l = 1; l <= 9; ++l) {
+        const double el = std::exp(-l * x), L = l;
+        poly += el * (6.0 / (L * L * L * L) + 6.0 * x / (L * L * L) + 3.0 * x * x / (L * L) + x * x * x / L);
+    }
+    poly = 1.0 - norm * poly;
+    return std::min(taylor, poly);
+}
+
+static double oracle_rosseland_r(double x, double b) {
+    const double pi = 3.14159265358979323846;
+    if (x > std::pow(1.7976931348623157e308, 0.25)) return b;
+    return b - 0.25 * (15.0 / (pi * pi * pi * pi)) * std::pow(x, 4) / std::expm1(x);
+}
+
+static void oracle_spectrum(const double* bounds, int G, double T, int kind, double* out) {
+    double prev = 0.0;
+    for (int g = 0; g < G - 1; ++g) {
+        const double x = bounds[g + 1] / T;
+        double f = oracle_planck_b(x);
+        if (kind == 1) f = oracle_rosseland_r(x, f);
+        out[g] = f - prev;
+        prev = f;
+    }
+    out[G - 1] = 1.0 - prev;
+}
+
+void oracle_planck_spectrum(const double* bounds, int G, double T, int kind, double* out) {
+    oracle_spectrum(bounds, G, T, kind, out);
+}
+
+// PlanckEmissionNonlinearForm::Mult / GetGradient (trt_integrators.cpp:56-152,
+// 229-302) at rule order 2p + 1; sigma per cell [G][Ne].
+void oracle_planck_emission(void* h, const double* bounds, const double* sigma, const double* T, double K,
+                            double* emission, double* grad) {
+    const Oracle& o = *static_cast<Oracle*>(h);
+    const int n = o.n, dim = o.dim, G = o.G;
+    const auto rule = tensor_rule(dim, gauss_legendre(o.p + 1));
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < o.ne; ++e) {
+        std::vector<double> phi(n), bs(G), rs(G);
+        for (int g = 0; g < G; ++g)
+            for (int i = 0; i < n; ++i) {
+                if (emission) emission[(size_t)g * o.ndof() + (size_t)e * n + i] = 0.0;
+                if (grad) for (int j = 0; j < n; ++j) grad[(((size_t)g * o.ne + e) * n + i) * n + j] = 0.0;
+            }
+        for (const auto& q : rule) {
+            double J[3][3], A[3][3];
+            geometry(o, e, q.xi, J, nullptr);
+            const double w = det_adj(dim, J, A) * q.w;
+            basis(o, q.xi, phi.data(), nullptr);
+            double Tq = 0.0;
+            for (int i = 0; i < n; ++i) Tq += T[(size_t)e * n + i] * phi[i];
+            oracle_spectrum(bounds, G, Tq, 0, bs.data());
+            oracle_spectrum(bounds, G, Tq, 1, rs.data());
+            for (int g = 0; g < G; ++g) {
+                const double sg = sigma[(size_t)g * o.ne + e];
+                if (emission) {
+                    const double c = w * K * std::pow(Tq, 4) * bs[g] * sg;
+                    for (int i = 0; i < n; ++i) emission[(size_t)g * o.ndof() + (size_t)e * n + i] += c * phi[i];
+                }
+                if (grad) {
+                    const double c = sg * rs[g] * w * 4.0 * K * std::pow(Tq, 3);
+                    for (int i = 0; i < n; ++i)
+                        for (int j = 0; j < n; ++j) grad[(((size_t)g * o.ne + e) * n + i) * n + j] += c * phi[i] * phi[j];
+                }
+            }
+        }
+    }
+}
+
+// meb_form of exe/scallion.cpp:755-765: GrayPlanckEmissionNFI at order 2p + 2
+// (trt_integrators.cpp:154-208) plus MassIntegrator(cv_dt); residual and the
+// gradient blocks [Ne][n][n].
+void oracle_energy_balance(void* h, const double* bounds, const double* sigma, const double* T, double K, double cv_dt,
+                           double* residual, double* grad) {
+    Oracle& o = *static_cast<Oracle*>(h);
+    if (o.Mt.empty()) assemble_time_mass(o);
+    const int n = o.n, nn = n * n, dim = o.dim, G = o.G;
+    const auto rule = tensor_rule(dim, gauss_legendre(o.p + 2));
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < o.ne; ++e) {
+        std::vector<double> phi(n), bs(G), rs(G), res(n, 0.0), gr(nn, 0.0);
+        const double* Te = T + (size_t)e * n;
+        for (const auto& q : rule) {
+            double J[3][3], A[3][3];
+            geometry(o, e, q.xi, J, nullptr);
+            const double w = det_adj(dim, J, A) * q.w;
+            basis(o, q.xi, phi.data(), nullptr);
+            double Tq = 0.0;
+            for (int i = 0; i < n; ++i) Tq += Te[i] * phi[i];
+            oracle_spectrum(bounds, G, Tq, 0, bs.data());
+            oracle_spectrum(bounds, G, Tq, 1, rs.data());
+            double sb = 0.0, sr = 0.0;
+            for (int g = 0; g < G; ++g) {
+                sb += sigma[(size_t)g * o.ne + e] * bs[g];
+                sr += sigma[(size_t)g * o.ne + e] * rs[g];
+            }
+            for (int i = 0; i < n; ++i) res[i] += w * K * std::pow(Tq, 4) * sb * phi[i];
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) gr[i * n + j] += sr * 4.0 * K * std::pow(Tq, 3) * w * phi[i] * phi[j];
+        }
+        const double* Mt = &o.Mt[(size_t)e * nn];
+        for (int i = 0; i < n; ++i) {
+            double m = 0.0;
+            for (int j = 0; j < n; ++j) m += Mt[i * n + j] * Te[j];
+            if (residual) residual[(size_t)e * n + i] = res[i] + cv_dt * m;
+            if (grad)
+                for (int j = 0; j < n; ++j) grad[((size_t)e * n + i) * n + j] = gr[i * n + j] + cv_dt * Mt[i * n + j];
+        }
+    }
+}
+
+// out = q + tau Mt psi_prev per (g, a, e) block (tvector.cpp:76-95, scallion.cpp:1358-1359)
+void oracle_time_source(void* h, const double* psi_prev, const double* q, double tau, double* out) {
+    Oracle& o = *static_cast<Oracle*>(h);
+    if (o.Mt.empty()) assemble_time_mass(o);
+    const int n = o.n;
+    const long long blocks = (long long)o.G * o.Nw * o.ne;
+#pragma omp parallel for schedule(static)
+    for (long long b = 0; b < blocks; ++b) {
+        const int e = (int)(b % o.ne);
+        const double* M = &o.Mt[(size_t)e * n * n];
+        std::vector<double> x(psi_prev + b * n, psi_prev + (b + 1) * n);
+        for (int i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < n; ++j) acc += M[i * n + j] * x[j];
+            out[b * n + i] = (q ? q[b * n + i] : 0.0) + tau * acc;
+        }
+    }
+}
+
+// unit MGMassIntegrator matrix of cell e (rule order 2p), row major
+static void oracle_unit_mass_cell(const Oracle& o, int e, double* M) {
+    const int n = o.n, dim = o.dim;
+    const auto rule = tensor_rule(dim, gauss_legendre(o.p + 1));
+    std::vector<double> phi(n);
+    for (int k = 0; k < n * n; ++k) M[k] = 0.0;
+    for (const auto& q : rule) {
+        double J[3][3], A[3][3];
+        geometry(o, e, q.xi, J, nullptr);
+        const double w = det_adj(dim, J, A) * q.w;
+        basis(o, q.xi, phi.data(), nullptr);
+        for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) M[i * n + j] += w * phi[i] * phi[j];
+    }
+}
+
+// which = 1: unit sigma mass, 2: MassIntegrator mass; y = M x per cell (Ndof)
+void oracle_mass_apply(void* h, int which, const double* x, double* y) {
+    Oracle& o = *static_cast<Oracle*>(h);
+    if (which == 2 && o.Mt.empty()) assemble_time_mass(o);
+    const int n = o.n;
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < o.ne; ++e) {
+        std::vector<double> Mu(n * n);
+        const double* M = &o.Mt[0];
+        if (which == 1) { oracle_unit_mass_cell(o, e, Mu.data()); M = Mu.data(); }
+        else M = &o.Mt[(size_t)e * n * n];
+        for (int i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < n; ++j) acc += M[i * n + j] * x[(size_t)e * n + j];
+            y[(size_t)e * n + i] = acc;
+        }
+    }
+}
+
+// sum_g sigma_g M phi_g (Mtot_collapse, scallion.cpp:786-797)
+void oracle_absorption(void* h, const double* sigma, const double* phi, double* y) {
+    const Oracle& o = *static_cast<Oracle*>(h);
+    const int n = o.n;
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < o.ne; ++e) {
+        std::vector<double> Mu(n * n);
+        oracle_unit_mass_cell(o, e, Mu.data());
+        for (int i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int g = 0; g < o.G; ++g) {
+                double m = 0.0;
+                for (int j = 0; j < n; ++j) m += Mu[i * n + j] * phi[(size_t)g * o.ndof() + (size_t)e * n + j];
+                acc += sigma[(size_t)g * o.ne + e] * m;
+            }
+            y[(size_t)e * n + i] = acc;
+        }
+    }
+}
+
+// sigma[g][e] = C nu_g^a T(centre)^b (opacity.cpp:47-63 at the group midpoints, piecewise constant)
+void oracle_powerlaw_opacity(void* h, const double* T, const double* nu, double C, double a, double b, double* sigma) {
+    const Oracle& o = *static_cast<Oracle*>(h);
+    const int n = o.n;
+    const double xc[3] = {0.5, 0.5, 0.5};
+    std::vector<double> phi(n);
+    basis(o, xc, phi.data(), nullptr);
+    for (int e = 0; e < o.ne; ++e) {
+        double Tc = 0.0;
+        for (int i = 0; i < n; ++i) Tc += phi[i] * T[(size_t)e * n + i];
+        for (int g = 0; g < o.G; ++g) sigma[(size_t)g * o.ne + e] = C * std::pow(nu[g], a) * std::pow(Tc, b);
+    }
 }
 
 }  // extern "C"
