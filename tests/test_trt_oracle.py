@@ -76,3 +76,59 @@ def test_oracle_trt_step_heats_from_the_inflow():
         assert np.all(o.T > 0)
         assert np.allclose(Tc, Tc[::-1], rtol=1e-10)
     assert first[0] > 1.1e-2 and first[2] > first[1] > first[0]
+
+
+def _oracle_cells(dim=2, p=1, G=6, jitter=0.0):
+    from oracle.oracle import OracleSweep
+    mesh = M.cartesian((3,) * dim, jitter=jitter, seed=5)
+    quad = Q.level_symmetric(4, dim)
+    sig = np.ones((G, mesh.num_elements))
+    return mesh, OracleSweep(mesh, p, quad, sig)
+
+
+def test_emission_sums_to_gray_emission():
+    # sum_g b_g = 1: with a group-independent opacity and a cellwise-constant T
+    # the multigroup emission sums to sigma ac T^4 int phi_i, which the
+    # energy-balance residual (another rule) also gives for cv_dt = 0
+    mesh, o = _oracle_cells(G=6)
+    bounds, _ = log_spaced_groups(1e-2, 10.0, 6)
+    ne, n = mesh.num_elements, o.n
+    Tc = np.linspace(0.3, 2.0, ne)
+    T = np.repeat(Tc, n)
+    sigma = np.tile(np.linspace(1.0, 3.0, ne), (6, 1))
+    em, _ = o.planck_emission(bounds, sigma, T, ac=1.7)
+    gray = em.reshape(6, ne * n).sum(axis=0)
+    ones = o.mass_apply(1, np.ones(ne * n))          # int phi_i (sum_j M_ij)
+    ref = np.repeat(sigma[0] * 1.7 * Tc ** 4, n) * ones
+    assert np.max(np.abs(gray - ref)) < 1e-13 * np.max(np.abs(ref))
+    res, _ = o.energy_balance(bounds, sigma, T, 1.7, 0.0)
+    assert np.max(np.abs(res - ref)) < 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("dim,p", [(2, 1), (2, 2), (3, 1)])
+def test_emission_gradients_are_derivatives(dim, p):
+    # d/dT [T^4 b_g(E/T)] = 4 T^3 r_g(E/T): the Rosseland-weighted blocks of
+    # PlanckEmissionNFI::AssembleElementGrad and the gray gradient are the
+    # Jacobians of the emission and of the energy-balance residual
+    mesh, o = _oracle_cells(dim, p, G=5, jitter=0.2)
+    bounds, _ = log_spaced_groups(1e-2, 10.0, 5)
+    ne, n = mesh.num_elements, o.n
+    rng = np.random.default_rng(9)
+    T = rng.uniform(0.3, 1.5, ne * n)
+    sigma = 10.0 ** rng.uniform(-1, 1, size=(5, ne))
+    _, dB = o.planck_emission(bounds, sigma, T, ac=1.0)
+    _, dBt = o.energy_balance(bounds, sigma, T, 1.0, 2.0)
+    h = 1e-6
+    for e in (0, ne - 1):
+        for j in range(n):
+            Tp, Tm = T.copy(), T.copy()
+            Tp[e * n + j] += h
+            Tm[e * n + j] -= h
+            ep, _ = o.planck_emission(bounds, sigma, Tp, ac=1.0)
+            em_, _ = o.planck_emission(bounds, sigma, Tm, ac=1.0)
+            fd = ((ep - em_) / (2 * h)).reshape(5, ne, n)[:, e, :]
+            assert np.max(np.abs(fd - dB[:, e, :, j])) < 1e-6 * np.max(np.abs(dB[:, e]))
+            rp, _ = o.energy_balance(bounds, sigma, Tp, 1.0, 2.0)
+            rm, _ = o.energy_balance(bounds, sigma, Tm, 1.0, 2.0)
+            fd = ((rp - rm) / (2 * h)).reshape(ne, n)[e]
+            assert np.max(np.abs(fd - dBt[e, :, j])) < 1e-6 * np.max(np.abs(dBt[e]))
