@@ -76,6 +76,10 @@ EXPORTS = {
     "allium_sweep_time_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
     "allium_sweep_powerlaw_opacity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                                 C.c_void_p]),
+    "allium_sweep_dsa_setup": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "allium_sweep_dsa_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_dsa_jacobi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_dsa_blocks": (C.c_int, [C.c_void_p, C.c_void_p]),
     "allium_sweep_synchronize": (C.c_int, [C.c_void_p]),
     "allium_sweep_last_error": (C.c_char_p, [C.c_void_p]),
     "allium_status_string": (C.c_char_p, [C.c_int]),

@@ -1,4 +1,5 @@
 // C ABI of liballium_sweep.so (declared in include/allium_sweep.h).
+#include <cmath>
 #include <cstdint>
 #include <initializer_list>
 #include <cstdio>
@@ -67,7 +68,7 @@ void free_all(Handle& h) {
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
                     h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts,
-                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu};
+                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu, h.d_orient, h.d_dsa, h.d_dsa_inv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -161,6 +162,7 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     STEP(upload(h, topo.slots.data(), topo.slots.size(), &h.d_slots));
     STEP(upload(h, topo.face_e1k1.data(), topo.face_e1k1.size(), &h.d_face_e1k1));
     STEP(upload(h, topo.nbrmap.data(), topo.nbrmap.size(), &h.d_nbrmap));
+    STEP(upload(h, topo.orient.data(), topo.orient.size(), &h.d_orient));
     STEP(upload(h, sigma_t, (size_t)h.G * h.ne, &h.d_sigma));
     CSTEP(cudaMalloc(&h.d_normals, (size_t)h.nfaces * h.dim * sizeof(double)));
     CSTEP(cudaMalloc(&h.d_dots, (size_t)h.nfaces * h.Nw * sizeof(double)));
@@ -719,6 +721,58 @@ int allium_sweep_powerlaw_opacity(allium_sweep* s, const double* T, const double
     if (int st = device_only(h, {T, sigma_out}, "allium_sweep_powerlaw_opacity")) return st;
     if (int st = upload(h, nu, (size_t)h.G, &h.d_nu)) return st;
     CUDA_OR_FAIL(h, allium::launch_powerlaw_opacity(h, T, h.d_nu, C, a, b, sigma_out));
+    return ALLIUM_OK;
+}
+
+// ------------------------------------------------------------ MIP diffusion (DSA)
+int allium_sweep_dsa_setup(allium_sweep* s, const double* sigma_s, double kappa, double penalty_min, double alpha_bdr,
+                           double tau) {
+    if (!s || !sigma_s) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!allium::dsa_supported(h)) {
+        h.last_error = "allium_sweep_dsa_setup: at most 16 DOFs per cell and no lumping";
+        return ALLIUM_ERR_UNSUPPORTED;
+    }
+    if (kappa < 0.0) kappa = (double)(h.p + 1) * (h.p + 1);
+    if (penalty_min < 0.0) {
+        // ComputeAlpha(quad, e_x) / 2 (src/angular_quadrature.cpp:266-276, exe/chive.cpp:669)
+        double a = 0.0, w = 0.0;
+        for (int q = 0; q < h.Nw; ++q) { a += std::fabs(h.h_omega[(size_t)q * h.dim]) * h.h_weights[q]; w += h.h_weights[q]; }
+        penalty_min = 0.5 * a / w;
+    }
+    if (alpha_bdr < 0.0) alpha_bdr = 0.5;
+    if (int st = upload(h, sigma_s, (size_t)h.G * h.ne, &h.d_sigma_s)) return st;
+    if (int st = ensure_mass2(h)) return st;
+    CUDA_OR_FAIL(h, allium::launch_dsa_assemble(h, h.d_sigma_s, kappa, penalty_min, alpha_bdr, tau));
+    h.dsa_ready = true;
+    return check_status(h);
+}
+
+int allium_sweep_dsa_apply(allium_sweep* s, const double* x, double* y) {
+    if (!s || !x || !y) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!h.dsa_ready) { h.last_error = "allium_sweep_dsa_setup has not been called"; return ALLIUM_ERR_ARG; }
+    if (int st = device_only(h, {x, y}, "allium_sweep_dsa_apply")) return st;
+    CUDA_OR_FAIL(h, allium::launch_dsa_apply(h, x, y));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_dsa_jacobi(allium_sweep* s, const double* x, double* y) {
+    if (!s || !x || !y) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!h.dsa_ready) { h.last_error = "allium_sweep_dsa_setup has not been called"; return ALLIUM_ERR_ARG; }
+    if (int st = device_only(h, {x, y}, "allium_sweep_dsa_jacobi")) return st;
+    CUDA_OR_FAIL(h, allium::launch_block_apply(h, h.d_dsa_inv, h.G, x, h.ndof, y, 1.0, 0));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_dsa_blocks(allium_sweep* s, double* out) {
+    if (!s || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (!h.dsa_ready) { h.last_error = "allium_sweep_dsa_setup has not been called"; return ALLIUM_ERR_ARG; }
+    const size_t count = (size_t)h.G * h.ne * (1 + h.nface) * h.n * h.n;
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(out, h.d_dsa, count * sizeof(double), cudaMemcpyDefault, h.stream));
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
     return ALLIUM_OK;
 }
 

@@ -22,8 +22,9 @@ struct RefTables {
     // 1D rules: 0 = sigma mass, 1 = convection, 2 = time mass, 3 = face mass,
     //           4 = source domain, 5 = source boundary, 6 = Planck emission
     //           (order 2p + 1), 7 = gray emission (order 2p + 2)
-    int rn[8];
-    double rx[8][kMaxRule], rw[8][kMaxRule];
+    //           8 = diffusion stiffness (order 2p + dim - 1)
+    int rn[9];
+    double rx[9][kMaxRule], rw[9][kMaxRule];
 };
 
 // Per (cell, local face) topology.  nbr >= 0: interior face; nbr = -1:
@@ -31,6 +32,13 @@ struct RefTables {
 // side = 0 when the cell is the face's element 1 (lower index).
 struct Slot {
     int face, nbr, side, attr;
+};
+
+// How the neighbour across a face sees it: its local face k2 and the map of
+// this cell's face coordinates t in [0,1]^(dim-1) to the neighbour's,
+// s_j = b_j + sum_c c[j][c] t_c.
+struct FaceOrient {
+    int8_t k2, b0, b1, c00, c01, c10, c11, pad;
 };
 
 struct Handle {
@@ -58,6 +66,7 @@ struct Handle {
     Slot* d_slots = nullptr;
     int* d_face_e1k1 = nullptr;      // [nfaces][2]
     uint8_t* d_nbrmap = nullptr;
+    FaceOrient* d_orient = nullptr;   // [ne][2 dim]
     double *d_G = nullptr, *d_M = nullptr, *d_Mt = nullptr, *d_F = nullptr, *d_sigma = nullptr;
     float *f_G = nullptr, *f_M = nullptr, *f_Mt = nullptr, *f_F = nullptr, *f_sigma = nullptr;
     int* d_level = nullptr;          // [ne*Nw]
@@ -92,6 +101,12 @@ struct Handle {
     int nrefl = 0;
     int* d_refl = nullptr;           // [nrefl][Nw] reflected angle feeding each entering angle
     int* d_feed = nullptr;           // [nrefl][Nw] entering angle fed by each angle
+
+    // MIP diffusion (DSA) operator: blocks [G][Ne][1 + 2 dim][n][n] (self,
+    // then the neighbour across each local face) and inverted self blocks
+    double* d_dsa = nullptr;
+    double* d_dsa_inv = nullptr;
+    bool dsa_ready = false;
 
     // thermal radiative transfer inputs (group bounds, group midpoints)
     double* d_bounds = nullptr;      // [G + 1]
@@ -165,6 +180,7 @@ struct Topology {
     std::vector<uint8_t> nbrmap;      // [ne][2 dim][nf]
     std::vector<double> corners;      // [ne][2^dim][dim], corner order c = c0 + 2 c1 + 4 c2
     std::vector<int> refl_faces;      // face id of reflective boundary face c
+    std::vector<FaceOrient> orient;   // [ne][2 dim], interior slots only
 };
 int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string& err);
 void mark_reflective(Topology& t, int nface, const std::vector<int>& refl_attrs);
@@ -185,6 +201,12 @@ cudaError_t launch_absorption(Handle& h, const double* sigma, const double* phi,
 cudaError_t launch_time_source(Handle& h, const double* psi_prev, const double* q, double tau, double* out);
 cudaError_t launch_powerlaw_opacity(Handle& h, const double* T, const double* nu, double C, double a, double b,
                                     double* sigma);
+
+// MIP diffusion operator for DSA (dsa.cu)
+bool dsa_supported(const Handle& h);
+cudaError_t launch_dsa_assemble(Handle& h, const double* sigma_s, double kappa, double penalty_min, double alpha_bdr,
+                                double tau);
+cudaError_t launch_dsa_apply(Handle& h, const double* x, double* y);
 cudaError_t launch_time_mass(Handle& h);
 int compute_levels(Handle& h);   // returns an allium status
 cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out);

@@ -102,6 +102,8 @@ RefTables make_ref_tables(int dim, int p, int lump) {
     // IntRules.Get(geom, 2p + 1) and (geom, 2p + 2): n = order / 2 + 1 points
     set_rule(t, 6, p + 1, false);
     set_rule(t, 7, p + 2, false);
+    // DiffusionIntegrator on tensor elements: order 2p + dim - 1
+    set_rule(t, 8, (2 * p + dim - 1) / 2 + 1, false);
     return t;
 }
 

@@ -77,6 +77,7 @@ int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string&
     out.slots.assign((size_t)ne * nface, Slot{-1, -1, 0, 0});
     out.face_e1k1.clear();
     out.nbrmap.assign((size_t)ne * nface * nf, 0);
+    out.orient.assign((size_t)ne * nface, FaceOrient{0, 0, 0, 0, 0, 0, 0, 0});
     int nfaces = 0;
     for (size_t i = 0; i < sorted.size();) {
         size_t j = i + 1;
@@ -113,6 +114,11 @@ int build_topology(const allium_mesh_desc& m, int p, Topology& out, std::string&
                     if (mc < 0) { err = "face vertices do not match"; return ALLIUM_ERR_MESH; }
                     for (int jj = 0; jj < td; ++jj) C[jj][c] = ((mc >> jj) & 1) - bvec[jj];
                 }
+                FaceOrient& fo = out.orient[(size_t)s.e * nface + s.k];
+                fo.k2 = (int8_t)o.k;
+                fo.b0 = (int8_t)bvec[0]; fo.b1 = (int8_t)bvec[1];
+                fo.c00 = (int8_t)C[0][0]; fo.c01 = (int8_t)C[0][1];
+                fo.c10 = (int8_t)C[1][0]; fo.c11 = (int8_t)C[1][1];
                 const int oa = o.k / 2, os = o.k % 2;
                 uint8_t* map = &out.nbrmap[((size_t)s.e * nface + s.k) * nf];
                 for (int q = 0; q < nf; ++q) {

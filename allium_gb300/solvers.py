@@ -16,7 +16,9 @@ src/transport_op.hpp:9-35).  Provided here:
   whose operator applies the FP32 sweep (moments accumulated in FP64); phi += d.
 
 All vectors are torch float64 CUDA tensors of length G * Ndof (phi) or
-G * Nw * Ndof (psi).  No diffusion synthetic acceleration is applied.
+G * Nw * Ndof (psi).  Diffusion synthetic acceleration (allium_gb300.dsa) is
+optional: the preconditioner of source iteration and the right preconditioner
+of GMRES.
 """
 from __future__ import annotations
 
@@ -97,8 +99,11 @@ class SolveResult:
     sweeps32: int = 0
 
 
-def source_iteration(op: SchurOperator, q, tol=1e-8, maxiter=10000, phi0=None):
-    """phi_{k+1} = D L^{-1} (D^T S phi_k + q); stop on ||phi_{k+1} - phi_k|| < tol ||phi_{k+1}||."""
+def source_iteration(op: SchurOperator, q, tol=1e-8, maxiter=10000, phi0=None, dsa=None):
+    """phi_{k+1/2} = D L^{-1} (D^T S phi_k + q); with dsa (a DSAPreconditioner)
+    phi_{k+1} = phi_k + P (phi_{k+1/2} - phi_k), P = I + K^{-1} M_s (SLISolver
+    with the DSA preconditioner, src/linalg.cpp:103-153); stop on
+    ||phi_{k+1} - phi_k|| < tol ||phi_{k+1}||."""
     t0 = time.perf_counter()
     L, D = op.L, op.D
     phi = torch.zeros(op.n, dtype=torch.float64, device=op.psi.device) if phi0 is None else phi0.clone()
@@ -111,6 +116,10 @@ def source_iteration(op: SchurOperator, q, tol=1e-8, maxiter=10000, phi0=None):
         L.Mult(op.psi, op.psi)
         op.sweeps64 += 1
         D.Mult(op.psi, new)
+        if dsa is not None:
+            r = new - phi
+            dsa(r, r)
+            torch.add(phi, r, out=new)
         it += 1
         change = (torch.linalg.norm(new - phi) / torch.linalg.norm(new)).item()
         hist.append(change)
@@ -122,9 +131,11 @@ def source_iteration(op: SchurOperator, q, tol=1e-8, maxiter=10000, phi0=None):
     return SolveResult(phi, it, conv, hist, time.perf_counter() - t0, op.sweeps64, op.sweeps32)
 
 
-def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0):
+def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=None):
     """Restarted GMRES on torch vectors; stops when ||b - A x|| <= max(tol ||b||, atol)
-    (the Arnoldi residual estimate).  Returns (x, iterations, history)."""
+    (the Arnoldi residual estimate).  prec(v, out) is a right preconditioner,
+    kept in flexible form (the preconditioned directions are stored), so it
+    may be an inner iterative solve.  Returns (x, iterations, history)."""
     dev, n = b.device, b.numel()
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     bnorm = torch.linalg.norm(b).item()
@@ -132,6 +143,7 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0):
         return x, 0, [0.0]
     target = max(tol * bnorm, atol)
     V = torch.empty((restart + 1, n), dtype=b.dtype, device=dev)
+    Z = torch.empty((restart, n), dtype=b.dtype, device=dev) if prec is not None else None
     w = torch.empty_like(b)
     hist = []
     it = 0
@@ -149,7 +161,11 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0):
         g[0] = beta
         k_used = 0
         for k in range(restart):
-            apply(V[k], w)
+            if prec is not None:
+                prec(V[k], Z[k])
+                apply(Z[k], w)
+            else:
+                apply(V[k], w)
             it += 1
             # classical Gram-Schmidt, twice
             h = torch.mv(V[: k + 1], w)
@@ -177,7 +193,8 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0):
             if abs(g[k + 1]) <= target or it >= maxiter or hn == 0.0:
                 break
         y = np.linalg.solve(np.triu(H[:k_used, :k_used]), g[:k_used])
-        x += torch.mv(V[:k_used].t(), torch.from_numpy(y).to(dev))
+        basis = Z if prec is not None else V
+        x += torch.mv(basis[:k_used].t(), torch.from_numpy(y).to(dev))
         apply(x, w)
         r = b - w
         beta = torch.linalg.norm(r).item()
@@ -185,26 +202,26 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0):
     return x, it, hist
 
 
-def solve_gmres(op: SchurOperator, q, tol=1e-8, restart=30, maxiter=2000):
-    """Plain FP64 GMRES on T phi = b."""
+def solve_gmres(op: SchurOperator, q, tol=1e-8, restart=30, maxiter=2000, prec=None):
+    """FP64 GMRES on T phi = b (prec: a right preconditioner such as DSA)."""
     t0 = time.perf_counter()
     b = op.rhs(q)
-    phi, it, hist = gmres(op.apply, b, tol=tol, restart=restart, maxiter=maxiter)
+    phi, it, hist = gmres(op.apply, b, tol=tol, restart=restart, maxiter=maxiter, prec=prec)
     torch.cuda.synchronize()
     conv = hist[-1] <= tol
     return SolveResult(phi, it, conv, hist, time.perf_counter() - t0, op.sweeps64, op.sweeps32)
 
 
-def refine(op: SchurOperator, q, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=20, inner_maxiter=500):
+def refine(op: SchurOperator, q, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=20, inner_maxiter=500, prec=None):
     """FP32-inner / FP64-outer iterative refinement on T phi = b."""
     t0 = time.perf_counter()
     res = refine_rhs(op, op.rhs(q), tol=tol, inner_tol=inner_tol, restart=restart, max_outer=max_outer,
-                     inner_maxiter=inner_maxiter)
+                     inner_maxiter=inner_maxiter, prec=prec)
     res.seconds = time.perf_counter() - t0
     return res
 
 
-def refine_rhs(op, b, x0=None, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=20, inner_maxiter=500):
+def refine_rhs(op, b, x0=None, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=20, inner_maxiter=500, prec=None):
     """Iterative refinement on T phi = b from phi = x0 (zero when None): the
     residual with op.apply (FP64 sweep), corrections by GMRES on op.apply32."""
     t0 = time.perf_counter()
@@ -231,7 +248,7 @@ def refine_rhs(op, b, x0=None, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=2
         if rel <= tol:
             conv = True
             break
-        d, it, _ = gmres(op.apply32, r, tol=inner_tol, restart=restart, maxiter=inner_maxiter)
+        d, it, _ = gmres(op.apply32, r, tol=inner_tol, restart=restart, maxiter=inner_maxiter, prec=prec)
         inner_total += it
         phi += d
         op.apply(phi, w)

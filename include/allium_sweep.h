@@ -300,6 +300,31 @@ int allium_sweep_time_source(allium_sweep* s, const double* psi_prev, const doub
 int allium_sweep_powerlaw_opacity(allium_sweep* s, const double* T, const double* nu, double C, double a, double b,
                                   double* sigma_out);
 
+/* ---- diffusion synthetic acceleration ----
+ * The MIP diffusion operator K of InteriorPenaltyDiscretization::GetOperator
+ * (src/moment_discretization.cpp:73-110, "scalar mip" in exe/chive.cpp:663-672):
+ * DiffusionIntegrator(1/(3 sigma_t)) + MassIntegrator(sigma_t - sigma_s) +
+ * MIPDiffusionIntegrator (src/moment_integrators.cpp:3-200; sigma = -1,
+ * penalty max(kappa {D/h}, penalty_min)) on interior faces +
+ * BoundaryMassIntegrator(alpha_bdr) on inflow boundaries (+ tau M), one
+ * operator per group on the handle's sigma_t.  Negative kappa, penalty_min or
+ * alpha_bdr select the reference defaults (p+1)^2, ComputeAlpha(quad, e_x)/2
+ * and 0.5.  sigma_s is [G][Ne] (host or device).  At most 16 DOFs per cell,
+ * no lumping. */
+int allium_sweep_dsa_setup(allium_sweep* s, const double* sigma_s, double kappa, double penalty_min, double alpha_bdr,
+                           double tau);
+
+/* y = K x on [G][Ndof] device vectors (the HypreParMatrix product). */
+int allium_sweep_dsa_apply(allium_sweep* s, const double* x, double* y);
+
+/* y = (block diagonal of K)^{-1} x: the block-Jacobi preconditioner of the
+ * diffusion solve (no reference counterpart: allium uses BoomerAMG). */
+int allium_sweep_dsa_jacobi(allium_sweep* s, const double* x, double* y);
+
+/* Copy K's blocks [G][Ne][1 + 2 dim][n][n] (self block, then the coupling to
+ * the neighbour across each local face) to out (host or device). */
+int allium_sweep_dsa_blocks(allium_sweep* s, double* out);
+
 /* Wait for the handle's stream; report sticky kernel errors and clear them. */
 int allium_sweep_synchronize(allium_sweep* s);
 

@@ -43,6 +43,7 @@ def lib():
         L.oracle_form_source.argtypes = [vp, dp, FN, dp, C.c_int, FN, dp]
         L.oracle_set_fixup.argtypes = [vp, C.c_int, C.c_double]
         L.oracle_set_reflective.argtypes = [vp, C.c_int, ip]
+        L.oracle_dsa_matrix.argtypes = [vp, dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, dp]
         L.oracle_planck_spectrum.argtypes = [dp, C.c_int, C.c_double, C.c_int, dp]
         L.oracle_planck_emission.argtypes = [vp, dp, dp, dp, C.c_double, dp, dp]
         L.oracle_energy_balance.argtypes = [vp, dp, dp, dp, C.c_double, C.c_double, dp, dp]
@@ -152,6 +153,18 @@ class OracleSweep:
         out = np.empty(self.G * self.ne)
         lib().oracle_powerlaw_opacity(self.h, _dp(_f64(T)), _dp(_f64(nu)), float(C0), float(a), float(b), _dp(out))
         return out.reshape(self.G, self.ne)
+
+    def dsa_matrix(self, sigma_s, g=0, kappa=None, penalty_min=None, alpha_bdr=0.5, tau=0.0, marshak=True):
+        """Dense MIP diffusion operator of group g (InteriorPenaltyDiscretization)."""
+        if kappa is None:
+            kappa = (self.order + 1) ** 2
+        if penalty_min is None:
+            w = self.quad.weights
+            penalty_min = 0.5 * float(np.sum(np.abs(self.quad.omega[:, 0]) * w) / np.sum(w))
+        K = np.empty((self.ndof, self.ndof))
+        lib().oracle_dsa_matrix(self.h, _dp(_f64(sigma_s)), int(g), float(kappa), float(penalty_min),
+                                float(alpha_bdr), float(tau), int(marshak), _dp(K))
+        return K
 
     def set_reflective(self, attributes):
         """Mark boundary attributes reflective (BoundaryCondition::REFLECTIVE)."""

@@ -1329,4 +1329,116 @@ void oracle_powerlaw_opacity(void* h, const double* T, const double* nu, double 
     }
 }
 
+
+// ---------------------------------------------------------------- MIP diffusion (DSA)
+// InteriorPenaltyDiscretization::GetOperator (moment_discretization.cpp:73-110)
+// as a dense matrix [Ndof][Ndof] for group g: DiffusionIntegrator(1/(3 sigma_t))
+// at order 2p + dim - 1, MassIntegrator(sigma_a) (+ tau) at the mass rule,
+// MIPDiffusionIntegrator face by face as moment_integrators.cpp:3-200 forms it
+// (elmat = -A + sigma A^T + J over the 2n x 2n face block, sigma = -1), and
+// BoundaryMassIntegrator(alpha_bdr) on non-reflective boundary faces when
+// marshak != 0.
+void oracle_dsa_matrix(void* h, const double* sigma_s, int g, double kappa, double penalty_min, double alpha_bdr,
+                       double tau, int marshak, double* K) {
+    Oracle& o = *static_cast<Oracle*>(h);
+    if (o.Mt.empty()) assemble_time_mass(o);
+    const int n = o.n, dim = o.dim, td = dim - 1;
+    const long long N = o.ndof();
+    for (long long q = 0; q < N * N; ++q) K[q] = 0.0;
+    auto D = [&](int e) { return 1.0 / (3.0 * o.sigma[(size_t)g * o.ne + e]); };
+    auto phys_grad = [&](int e, const double* xi, std::vector<double>& phi, std::vector<std::array<double, 3>>& gx) {
+        double J[3][3], A[3][3];
+        geometry(o, e, xi, J, nullptr);
+        const double det = det_adj(dim, J, A);
+        std::vector<std::array<double, 3>> dref(n);
+        basis(o, xi, phi.data(), reinterpret_cast<double(*)[3]>(dref.data()));
+        for (int i = 0; i < n; ++i)
+            for (int r = 0; r < dim; ++r) {
+                double v = 0.0;
+                for (int qq = 0; qq < dim; ++qq) v += A[qq][r] * dref[i][qq];
+                gx[i][r] = v / det;
+            }
+        return det;
+    };
+    std::vector<double> phi(n), phi2(n);
+    std::vector<std::array<double, 3>> gx(n), gx2(n);
+    // volume terms
+    const auto rule_d = tensor_rule(dim, gauss_legendre((2 * o.p + dim - 1) / 2 + 1));
+    for (int e = 0; e < o.ne; ++e) {
+        const long long off = (long long)e * n;
+        for (const auto& q : rule_d) {
+            const double det = phys_grad(e, q.xi, phi, gx);
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    double d = 0.0;
+                    for (int r = 0; r < dim; ++r) d += gx[i][r] * gx[j][r];
+                    K[(off + i) * N + off + j] += q.w * det * D(e) * d;
+                }
+        }
+        const double sa = o.sigma[(size_t)g * o.ne + e] - sigma_s[(size_t)g * o.ne + e];
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) K[(off + i) * N + off + j] += (sa + tau) * o.Mt[((size_t)e * n + i) * n + j];
+    }
+    // faces
+    const auto rule_f = tensor_rule(td, gauss_legendre(o.p + 1));
+    for (const Face& f : o.faces) {
+        if (f.e2 < 0) {
+            if (!marshak || !f.refl.empty()) continue;
+            const long long off = (long long)f.e1 * n;
+            for (const auto& q : rule_f) {
+                double xi[3], nr[3];
+                face_point(dim, f.k1, q.xi, xi);
+                raw_normal(o, f.e1, f.k1, xi, nr);
+                const double w = q.w * (dim == 1 ? 1.0 : norm(dim, nr));
+                basis(o, xi, phi.data(), nullptr);
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j) K[(off + i) * N + off + j] += alpha_bdr * w * phi[i] * phi[j];
+            }
+            continue;
+        }
+        const int n2 = 2 * n;
+        std::vector<double> elmat(n2 * n2, 0.0), jmat(n2 * n2, 0.0);
+        for (const auto& q : rule_f) {
+            double xi1[3], xi2[3], s2[2], nr[3];
+            face_point(dim, f.k1, q.xi, xi1);
+            e2_face_coords(f, td, q.xi, s2);
+            face_point(dim, f.k2, s2, xi2);
+            raw_normal(o, f.e1, f.k1, xi1, nr);      // scaled normal out of e1
+            const double nn = dotv(dim, nr, nr);
+            const double det1 = phys_grad(f.e1, xi1, phi, gx);
+            const double det2 = phys_grad(f.e2, xi2, phi2, gx2);
+            const double w1 = q.w / 2 * D(f.e1), w2 = q.w / 2 * D(f.e2);
+            std::vector<double> dn1(n), dn2(n);
+            for (int j = 0; j < n; ++j) {
+                dn1[j] = w1 * dotv(dim, gx[j].data(), nr);
+                dn2[j] = w2 * dotv(dim, gx2[j].data(), nr);
+            }
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    elmat[i * n2 + j] += phi[i] * dn1[j];
+                    elmat[i * n2 + n + j] += phi[i] * dn2[j];
+                    elmat[(n + i) * n2 + j] -= phi2[i] * dn1[j];
+                    elmat[(n + i) * n2 + n + j] -= phi2[i] * dn2[j];
+                }
+            double wq = kappa * (w1 * nn / det1 + w2 * nn / det2);
+            const double fl = penalty_min * q.w * std::sqrt(nn);
+            if (wq < fl) wq = fl;
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    jmat[i * n2 + j] += wq * phi[i] * phi[j];
+                    jmat[i * n2 + n + j] -= wq * phi[i] * phi2[j];
+                    jmat[(n + i) * n2 + j] -= wq * phi2[i] * phi[j];
+                    jmat[(n + i) * n2 + n + j] += wq * phi2[i] * phi2[j];
+                }
+        }
+        // elmat := -elmat + sigma elmat^T + jmat with sigma = -1
+        const long long off[2] = {(long long)f.e1 * n, (long long)f.e2 * n};
+        for (int i = 0; i < n2; ++i)
+            for (int j = 0; j < n2; ++j) {
+                const double v = -elmat[i * n2 + j] - elmat[j * n2 + i] + jmat[i * n2 + j];
+                K[(off[i / n] + i % n) * N + off[j / n] + j % n] += v;
+            }
+    }
+}
+
 }  // extern "C"
