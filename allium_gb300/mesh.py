@@ -119,3 +119,27 @@ def cartesian(cells, extents=None, jitter: float = 0.0, seed: int | None = None)
         offs = rng.uniform(-jitter, jitter, size=verts.shape) * h
         verts = verts + offs * interior[:, None]
     return Mesh(dim, verts, elems, bfaces, battr, cells)
+
+
+def disjoint_union(meshes):
+    """One mesh holding independent meshes side by side (no shared vertices, so
+    no shared faces): elements, vertices and boundary faces concatenated in
+    order.  Returns (mesh, element_offsets) with element_offsets[k] the first
+    element of meshes[k] and element_offsets[-1] the total."""
+    dim = meshes[0].dim
+    verts, elems, bfs, bas = [], [], [], []
+    voff, eoffs = 0, [0]
+    for m in meshes:
+        if m.dim != dim:
+            raise ValueError("meshes of one union must share the dimension")
+        verts.append(m.vertices)
+        elems.append(m.elements + voff)
+        bfs.append(m.boundary_faces + voff)
+        bas.append(m.boundary_attributes)
+        voff += m.num_vertices
+        eoffs.append(eoffs[-1] + m.num_elements)
+    mesh = Mesh(dim, np.ascontiguousarray(np.concatenate(verts), dtype=np.float64),
+                np.ascontiguousarray(np.concatenate(elems), dtype=np.int32),
+                np.ascontiguousarray(np.concatenate(bfs), dtype=np.int32),
+                np.ascontiguousarray(np.concatenate(bas), dtype=np.int32))
+    return mesh, np.array(eoffs, dtype=np.int64)

@@ -66,7 +66,10 @@ class SchurOperator:
         return out
 
     def apply32(self, x, out):
-        """T with the FP32 sweep on node-major vectors (contiguous runs per level)."""
+        """T with the FP32 sweep on node-major vectors (contiguous runs per level);
+        orders above 1 and reflective boundaries use allium's RIGHT layout."""
+        if self.L.order > 1 or getattr(self.L, "has_reflective", False):
+            return self.apply32_right(x, out)
         if self.psi32 is None:
             self.psi32 = torch.empty(self.L.width, dtype=torch.float32, device=self.psi.device)
         ScatteringSourceF32Nodes(self.L, self.sigma_s, x, None, self.psi32)

@@ -74,6 +74,7 @@ class InverseAdvectionOperator:
         fd = FeDesc(self.order, 0, self.lump)
         qd = QuadDesc(self.dim, self.Nw, om.ctypes.data, w.ctypes.data)
         bcd = None
+        self.has_reflective = bool(bc) and any(str(k).lower() == "reflective" for k in bc.values())
         if bc:
             kinds = {"inflow": 0, "reflective": 1}
             attrs = np.array(list(bc.keys()), dtype=np.int32)

@@ -260,6 +260,47 @@ def trt_section(steps):
     return out
 
 
+def batch_section(count):
+    """Batched uneven problems: `count` independent one-group 2D problems
+    (side U{16..256}, p U{1,2,3}, S4..S12, sigma_t 10^U[-1, log10 50] per cell,
+    c U[0.3, 0.99], q = 1, vacuum), each to 1e-8: one union handle per
+    (order, S_N) group, source iteration with MIP-DSA and FP32-inner /
+    FP64-outer refinement with DSA-preconditioned GMRES; then the same problems
+    one handle each (source iteration with DSA) for comparison."""
+    import torch
+    from allium_gb300.batch import ProblemGroup, random_problems, solve_batched
+    probs = random_problems(count, seed=SEED + 7)
+    warm = random_problems(6, seed=1, sides=(8, 16))
+    solve_batched(warm, "si")
+    solve_batched(warm, "ir")
+    out = {"problems": count, "entries": int(sum(p.mesh.num_elements * (p.order + 1) ** 2 * (p.sn * (p.sn + 2) // 2)
+                                              for p in probs))}
+    for method in ("si", "ir"):
+        res, groups = solve_batched(probs, method=method, tol=1e-8)
+        out["batched_" + method] = {"seconds": res.seconds, "setup_seconds": res.setup_seconds, "groups": res.groups,
+                                    "iterations_per_group": res.iterations, "converged": res.converged,
+                                    "fp64_sweeps": res.sweeps64, "fp32_sweeps": res.sweeps32}
+        del groups
+        torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    setup = solve = 0.0
+    conv = True
+    for p in probs:
+        a = time.perf_counter()
+        g = ProblemGroup([p])
+        torch.cuda.synchronize()
+        b = time.perf_counter()
+        _, _, c = g.solve_si(tol=1e-8)
+        torch.cuda.synchronize()
+        setup += b - a
+        solve += time.perf_counter() - b
+        conv = conv and c
+        del g
+    out["one_by_one_si"] = {"seconds": solve, "setup_seconds": setup, "converged": conv}
+    out["batching_speedup_si"] = solve / out["batched_si"]["seconds"]
+    return out
+
+
 def chive2d_section(cpu=True):
     """The 2D chive configuration: 64x64 quads, p = 1, S8, sigma_t = 1,
     sigma_s = 0.9, q = 1, vacuum; source iteration to 1e-8 relative change of
@@ -478,6 +519,8 @@ def run_gpu(args):
         line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0])
         line["chive_2d"] = chive2d_section(cpu=not args.no_cpu)
         line["trt_marshak"] = trt_section(args.trt_steps)
+        if args.batch_problems > 0:
+            line["batched_uneven"] = batch_section(args.batch_problems)
     if not args.no_cpu and tuple(cells) == CELLS:
         rates, size = cpu_sweep_sample(os.cpu_count() or 1, 3, 1)
         line["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": os.cpu_count(),
@@ -498,6 +541,7 @@ def main():
     ap.add_argument("--cells", type=int, default=CELLS[0], help="cells per axis (smaller cases for profiling)")
     ap.add_argument("--no-solve", action="store_true", help="skip the time-to-tolerance solves")
     ap.add_argument("--trt-steps", type=int, default=200, help="time steps of the multigroup TRT section")
+    ap.add_argument("--batch-problems", type=int, default=256, help="problems of the batched section (0 skips it)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

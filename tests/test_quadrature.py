@@ -57,3 +57,13 @@ def test_layouts():
     assert psi_index(0, 1, 6) == np.ravel_multi_index((0, 1, 6), (G, Nw, Ndof))
     mom_index = lambda g, m, i: i + Ndof * (g + G * m)
     assert mom_index(1, 2, 3) == 3 + 8 * (1 + 2 * 2)
+
+
+def test_disjoint_union():
+    from allium_gb300 import mesh as M
+    a, b = M.cartesian((2, 3)), M.cartesian((4, 1))
+    u, off = M.disjoint_union([a, b])
+    assert list(off) == [0, 6, 10]
+    assert u.num_vertices == a.num_vertices + b.num_vertices
+    assert np.array_equal(u.elements[6:], b.elements + a.num_vertices)
+    assert np.array_equal(u.boundary_attributes, np.concatenate([a.boundary_attributes, b.boundary_attributes]))
