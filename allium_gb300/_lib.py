@@ -80,6 +80,15 @@ EXPORTS = {
     "allium_sweep_dsa_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_dsa_jacobi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_dsa_blocks": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "allium_mlp_gemm": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_longlong, C.c_void_p,
+                                  C.c_longlong, C.c_longlong, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p,
+                                  C.c_float, C.c_float, C.c_int, C.c_void_p]),
+    "allium_mlp_relu_backward": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_mlp_bias_grad": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_mlp_mse_grad": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_mlp_adam": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                  C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]),
+    "allium_mlp_to_bf16": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_synchronize": (C.c_int, [C.c_void_p]),
     "allium_sweep_last_error": (C.c_char_p, [C.c_void_p]),
     "allium_status_string": (C.c_char_p, [C.c_int]),

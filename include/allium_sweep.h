@@ -325,6 +325,40 @@ int allium_sweep_dsa_jacobi(allium_sweep* s, const double* x, double* y);
  * the neighbour across each local face) to out (host or device). */
 int allium_sweep_dsa_blocks(allium_sweep* s, double* out);
 
+/* ---- learned initial iterate: per-cell MLP kernels (no reference counterpart) ----
+ * A small network predicts the next time step's moments from the current
+ * state; it only supplies the initial iterate of the outer solve, which still
+ * converges to the same tolerance.  Device pointers; stream is a cudaStream_t
+ * (NULL: the default stream).  BF16 operands (__nv_bfloat16 / torch.bfloat16),
+ * FP32 accumulation and outputs. */
+
+/* C[M][N] = alpha A B (+ beta C) (+ bias[N]) (ReLU if relu): A(m, k) at
+ * A[m sam + k sak], B(k, n) at B[k sbk + n sbn] (strides in elements, so
+ * transposed operands need no copy); C row stride ldc; C_bf16 receives a BF16
+ * copy when not NULL.  mma.sync m16n8k16 tensor-core tiles of 64 x 64. */
+int allium_mlp_gemm(int M, int N, int K, const void* A, long long sam, long long sak, const void* B, long long sbk,
+                    long long sbn, float* C, long long ldc, void* C_bf16, const float* bias, float alpha, float beta,
+                    int relu, void* stream);
+
+/* dz = dy where y > 0, else 0 (ReLU gradient); dz and/or its BF16 copy. */
+int allium_mlp_relu_backward(long long count, const float* dy, const float* y, float* dz, void* dz_bf16, void* stream);
+
+/* db[n] = sum_m dy[m][n]. */
+int allium_mlp_bias_grad(int M, int N, const float* dy, float* db, void* stream);
+
+/* dy = 2 (y - target) / count; loss_partials[ceil(count / 256)] receive the
+ * blocks' sums of squared errors. */
+int allium_mlp_mse_grad(long long count, const float* y, const float* target, float* dy, float* loss_partials,
+                        void* stream);
+
+/* One Adam step (step >= 1) on FP32 weights w with moments m, v; refreshes
+ * the BF16 copy w_bf16 when not NULL. */
+int allium_mlp_adam(long long count, float* w, void* w_bf16, const float* grad, float* m, float* v, float lr,
+                    float beta1, float beta2, float eps, int step, void* stream);
+
+/* y = bf16(x). */
+int allium_mlp_to_bf16(long long count, const float* x, void* y, void* stream);
+
 /* Wait for the handle's stream; report sticky kernel errors and clear them. */
 int allium_sweep_synchronize(allium_sweep* s);
 
