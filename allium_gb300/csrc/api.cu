@@ -68,7 +68,7 @@ void free_all(Handle& h) {
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
                     h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts,
-                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu, h.d_orient, h.d_dsa, h.d_dsa_inv, h.d_node_rec};
+                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu, h.d_orient, h.d_dsa, h.d_dsa_inv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);

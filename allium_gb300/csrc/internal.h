@@ -67,7 +67,6 @@ struct Handle {
     int* d_face_e1k1 = nullptr;      // [nfaces][2]
     uint8_t* d_nbrmap = nullptr;
     FaceOrient* d_orient = nullptr;   // [ne][2 dim]
-    int* d_node_rec = nullptr;        // per-node records of the node-major FP32 sweep (level order)
     double *d_G = nullptr, *d_M = nullptr, *d_Mt = nullptr, *d_F = nullptr, *d_sigma = nullptr;
     float *f_G = nullptr, *f_M = nullptr, *f_Mt = nullptr, *f_F = nullptr, *f_sigma = nullptr;
     int* d_level = nullptr;          // [ne*Nw]

@@ -22,8 +22,6 @@ cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi) {
 template <int D, int P>
 cudaError_t sweep_levels_nodes(Handle& h, const SweepArgs<float>& args, cudaStream_t stream) {
     constexpr int kBlock = 128;
-    constexpr int W = NodeRecord<D>::words;
-    const int4* rec = reinterpret_cast<const int4*>(h.d_node_rec);
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = h.h_level_offsets[l];
         const int count = h.h_level_offsets[l + 1] - off;
@@ -31,23 +29,7 @@ cudaError_t sweep_levels_nodes(Handle& h, const SweepArgs<float>& args, cudaStre
         const long long threads = (long long)count * h.G;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_nodes_rec<D, P><<<grid, kBlock, 0, stream>>>(args, rec + (size_t)off * (W / 4), count);
-    }
-    return cudaGetLastError();
-}
-
-// per-node records of the node-major sweep, built on first use
-cudaError_t ensure_node_records(Handle& h) {
-    if (h.d_node_rec) return cudaSuccess;
-    const int W = h.dim == 1 ? NodeRecord<1>::words : (h.dim == 2 ? NodeRecord<2>::words : NodeRecord<3>::words);
-    const long long total = (long long)h.ne * h.Nw;
-    cudaError_t e = cudaMalloc(&h.d_node_rec, (size_t)total * W * sizeof(int));
-    if (e != cudaSuccess) { h.d_node_rec = nullptr; return e; }
-    const unsigned grid = (unsigned)((total + 255) / 256);
-    switch (h.dim) {
-        case 1: k_node_records<1><<<grid, 256, 0, h.stream>>>((int)total, h.Nw, h.d_level_nodes, h.d_slots, h.f_dots, h.d_node_rec); break;
-        case 2: k_node_records<2><<<grid, 256, 0, h.stream>>>((int)total, h.Nw, h.d_level_nodes, h.d_slots, h.f_dots, h.d_node_rec); break;
-        default: k_node_records<3><<<grid, 256, 0, h.stream>>>((int)total, h.Nw, h.d_level_nodes, h.d_slots, h.f_dots, h.d_node_rec); break;
+        k_sweep_nodes<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count);
     }
     return cudaGetLastError();
 }
@@ -77,8 +59,6 @@ cudaError_t launch_sweep_nodes_f32(Handle& h, const float* src, float* psi) {
             }
         });
     }
-    cudaError_t re = ensure_node_records(h);
-    if (re != cudaSuccess) return re;
     return run_graph(h, 5, src, psi, [&](cudaStream_t st) -> cudaError_t {
         switch (h.dim * 10 + h.p) {
             case 10: return sweep_levels_nodes<1, 0>(h, a, st);

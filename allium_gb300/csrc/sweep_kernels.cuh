@@ -690,145 +690,6 @@ __global__ void __launch_bounds__(128, 4) k_sweep_nodes(SweepArgs<float> s, cons
     store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), b);
 }
 
-// Per-node records of the node-major sweep, in level order: cell, angle, the
-// oriented FP32 face dots and the neighbour across each face, padded to whole
-// int4 words, so a thread learns where its upwind traces are from one
-// contiguous read instead of the chain node -> slots -> face dots.
-template <int D>
-struct NodeRecord {
-    static constexpr int words = ((2 + 4 * D) + 3) / 4 * 4;
-};
-
-template <int D>
-__global__ void k_node_records(int total, int Nw, const int* __restrict__ nodes, const Slot* __restrict__ slots,
-                               const float* __restrict__ dots, int* __restrict__ rec) {
-    constexpr int NFACE = 2 * D, W = NodeRecord<D>::words;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= total) return;
-    const int node = nodes[t];
-    const int e = node / Nw, a = node - e * Nw;
-    int* r = rec + (size_t)t * W;
-    r[0] = e;
-    r[1] = a;
-    for (int k = 0; k < NFACE; ++k) {
-        const Slot q = slots[(size_t)e * NFACE + k];
-        const float d1 = dots[(size_t)q.face * Nw + a];
-        r[2 + k] = __float_as_int(q.side ? -d1 : d1);
-        r[2 + NFACE + k] = q.nbr;
-    }
-    for (int k = 2 + 2 * NFACE; k < W; ++k) r[k] = 0;
-}
-
-// FP32 node-major sweep from the records: upwind traces are gathered with the
-// neighbour's DOF map (one 32-bit map word per face for NF <= 4) and their
-// loads issued before the local assembly.
-template <int D, int P>
-__global__ void __launch_bounds__(128, 4) k_sweep_nodes_rec(SweepArgs<float> s, const int4* __restrict__ rec,
-                                                            int count) {
-    constexpr int N = ipow(P + 1, D);
-    constexpr int NF = ipow(P + 1, D - 1);
-    constexpr int NFACE = 2 * D;
-    constexpr int W = NodeRecord<D>::words;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count * s.G) return;
-    const int ni = t / s.G;
-    const int g = t - ni * s.G;
-    int w[W];
-#pragma unroll
-    for (int q = 0; q < W / 4; ++q) {
-        const int4 v = __ldg(rec + (size_t)ni * (W / 4) + q);
-        w[4 * q] = v.x; w[4 * q + 1] = v.y; w[4 * q + 2] = v.z; w[4 * q + 3] = v.w;
-    }
-    const int e = w[0], a = w[1];
-    float dots[NFACE];
-    int nbrs[NFACE];
-#pragma unroll
-    for (int k = 0; k < NFACE; ++k) { dots[k] = __int_as_float(w[2 + k]); nbrs[k] = w[2 + NFACE + k]; }
-    // upwind face values (gathered through the neighbour DOF map)
-    float u[NFACE][NF];
-#pragma unroll
-    for (int k = 0; k < NFACE; ++k) {
-        if (dots[k] < 0.0f && nbrs[k] >= 0) {
-            const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
-            const float* up = s.psi + node_index(s.Nw, s.G, N, nbrs[k], a, g);
-#pragma unroll
-            for (int jj = 0; jj < NF; ++jj) u[k][jj] = up[map[jj]];
-        } else {
-#pragma unroll
-            for (int jj = 0; jj < NF; ++jj) u[k][jj] = 0.0f;
-        }
-    }
-    float b[N];
-    load_block<N>(s.src + node_index(s.Nw, s.G, N, e, a, g), b);
-    // local matrix: sum_d Omega_d G_d + sigma M (+ tau Mt) + outflow faces
-    float A[N][N];
-    {
-        float om[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int d = 0; d < D; ++d) om[d] = s.omega[a * D + d];
-        const float* Gm = s.Gm + (size_t)e * D * N * N;
-        const float* M = s.M + (size_t)e * N * N;
-        const float sg = s.sigma[(size_t)g * s.ne + e];
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            float row[N], mrow[N];
-            load_block<N>(Gm + i * N, row);
-            load_block<N>(M + i * N, mrow);
-#pragma unroll
-            for (int j = 0; j < N; ++j) A[i][j] = om[0] * row[j];
-#pragma unroll
-            for (int d = 1; d < D; ++d) {
-                load_block<N>(Gm + d * N * N + i * N, row);
-#pragma unroll
-                for (int j = 0; j < N; ++j) A[i][j] = fmaf(om[d], row[j], A[i][j]);
-            }
-#pragma unroll
-            for (int j = 0; j < N; ++j) A[i][j] = fmaf(sg, mrow[j], A[i][j]);
-        }
-        if (s.td) {
-            const float* Mt = s.Mt + (size_t)e * N * N;
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                float row[N];
-                load_block<N>(Mt + i * N, row);
-#pragma unroll
-                for (int j = 0; j < N; ++j) A[i][j] = fmaf(s.tau, row[j], A[i][j]);
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < NFACE; ++k) {
-        const float* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
-        const float dk = dots[k];
-        if (dk > 0.0f) {
-#pragma unroll
-            for (int ii = 0; ii < NF; ++ii) {
-                float frow[NF];
-                load_block<NF>(F + ii * NF, frow);
-#pragma unroll
-                for (int jj = 0; jj < NF; ++jj) {
-                    const int fi = face_dof(D, P, k, ii), fj = face_dof(D, P, k, jj);
-                    A[fi][fj] = fmaf(dk, frow[jj], A[fi][fj]);
-                }
-            }
-        } else if (dk < 0.0f && nbrs[k] >= 0) {
-            const float rd = -dk;
-#pragma unroll
-            for (int ii = 0; ii < NF; ++ii) {
-                float frow[NF];
-                load_block<NF>(F + ii * NF, frow);
-                float acc = 0.0f;
-#pragma unroll
-                for (int jj = 0; jj < NF; ++jj) acc = fmaf(frow[jj], u[k][jj], acc);
-                const int fi = face_dof(D, P, k, ii);
-                b[fi] = fmaf(rd, acc, b[fi]);
-            }
-        }
-    }
-    if (!solve_local<N, false>(A, b)) atomicOr(s.status, kErrSingular);
-    store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), b);
-}
-
 // RIGHT (g, a, i) FP64 <-> node-major FP32, and the node-major scattering source / moments
 static __global__ void k_right_to_nodes(int ne, int Nw, int G, int N, long long ndof, const double* __restrict__ in,
                                  float* __restrict__ out) {
