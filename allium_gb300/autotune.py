@@ -1,0 +1,65 @@
+"""Launch-configuration autotuner for one sweep handle.
+
+The knobs are the schedule (wavefront levels, one launch per level captured
+in a CUDA graph, or the persistent dataflow kernel with per-node completion
+flags) and the threads per block of the thread-per-node level kernels, for
+the FP64 sweep and the FP32 sweep (node-major layout) separately.  Each
+candidate is timed with CUDA events over a few Mults after one untimed call
+(which captures its graph and, for FP64, builds the factor cache once), the
+fastest is kept and set on the handle.  Every candidate computes each node
+with the same arithmetic, so tuning changes speed only.
+"""
+from __future__ import annotations
+
+import torch
+
+
+def _time(fn, reps):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def autotune(L, reps=3, blocks=(32, 64, 128), fp32=True):
+    """Pick (schedule, FP64 block) on FP64 Mults and the FP32 node-layout block
+    on FP32 Mults; returns {"fp64": {...}, "fp32": {...}, "trials": [...]}."""
+    dev = torch.device("cuda")
+    src = torch.rand(L.width, dtype=torch.float64, device=dev)
+    psi = torch.empty_like(src)
+    schedules = [0]
+    if L.order <= 1 and not getattr(L, "has_reflective", False):
+        schedules.append(1)
+    trials = []
+    best = None
+    for sch in schedules:
+        L.SetSchedule(sch)
+        for b in (blocks if sch == 0 else (blocks[-1],)):
+            L.SetBlockSize(64, b)
+            ms = _time(lambda: L.Mult(src, psi), reps)
+            trials.append({"precision": 64, "schedule": sch, "block": b, "ms": ms})
+            if best is None or ms < best["ms"]:
+                best = trials[-1]
+    L.SetSchedule(best["schedule"])
+    L.SetBlockSize(64, best["block"])
+    out = {"fp64": best, "trials": trials}
+    if fp32 and L.order <= 1 and not getattr(L, "has_reflective", False):
+        f = torch.empty(L.width, dtype=torch.float32, device=dev)
+        L.ToNodeLayoutF32(src, f)
+        g = torch.empty_like(f)
+        best32 = None
+        for b in blocks:
+            L.SetBlockSize(32, b)
+            ms = _time(lambda: L.MultF32Nodes(f, g), reps)
+            trials.append({"precision": 32, "schedule": best["schedule"], "block": b, "ms": ms})
+            if best32 is None or ms < best32["ms"]:
+                best32 = trials[-1]
+        L.SetBlockSize(32, best32["block"])
+        out["fp32"] = best32
+    L.synchronize()
+    return out

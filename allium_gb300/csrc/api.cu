@@ -589,6 +589,18 @@ int allium_sweep_selftest_wait(allium_sweep* s, int poll_limit) {
     return check_status(h);
 }
 
+int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads) {
+    if (!s || (precision != 32 && precision != 64) || (threads != 32 && threads != 64 && threads != 128))
+        return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    int& b = precision == 64 ? h.block64 : h.block32;
+    if (b != threads) {
+        b = threads;
+        allium::drop_graphs(h);
+    }
+    return ALLIUM_OK;
+}
+
 int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum) {
     if (!s || kind < 0) return ALLIUM_ERR_ARG;
     Handle& h = s->h;

@@ -67,6 +67,8 @@ struct Handle {
     int* d_face_e1k1 = nullptr;      // [nfaces][2]
     uint8_t* d_nbrmap = nullptr;
     FaceOrient* d_orient = nullptr;   // [ne][2 dim]
+    // threads per block of the thread-per-node level kernels (FP64, FP32)
+    int block64 = 128, block32 = 128;
     double *d_G = nullptr, *d_M = nullptr, *d_Mt = nullptr, *d_F = nullptr, *d_sigma = nullptr;
     float *f_G = nullptr, *f_M = nullptr, *f_Mt = nullptr, *f_F = nullptr, *f_sigma = nullptr;
     int* d_level = nullptr;          // [ne*Nw]

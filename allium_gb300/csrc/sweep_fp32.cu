@@ -21,7 +21,7 @@ cudaError_t launch_sweep_fp32(Handle& h, const float* src, float* psi) {
 
 template <int D, int P>
 cudaError_t sweep_levels_nodes(Handle& h, const SweepArgs<float>& args, cudaStream_t stream) {
-    constexpr int kBlock = 128;
+    const int kBlock = h.block32;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = h.h_level_offsets[l];
         const int count = h.h_level_offsets[l + 1] - off;

@@ -1,13 +1,15 @@
 // Level-by-level launch of the sweep kernel for one arithmetic type.
 #pragma once
 
+#include <type_traits>
+
 #include "sweep_kernels.cuh"
 
 namespace allium {
 
 template <int D, int P, typename R, bool PIVOT>
 cudaError_t sweep_levels(Handle& h, const SweepArgs<R>& args, cudaStream_t stream) {
-    constexpr int kBlock = 128;
+    const int kBlock = std::is_same<R, double>::value ? h.block64 : h.block32;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = h.h_level_offsets[l];
         const int count = h.h_level_offsets[l + 1] - off;
@@ -48,7 +50,7 @@ cudaError_t factor_all(Handle& h, const SweepArgs<double>& args) {
 
 template <int D, int P, typename R>
 cudaError_t sweep_levels_cached(Handle& h, const SweepArgs<R>& args, const R* inv, cudaStream_t stream) {
-    constexpr int kBlock = 128;
+    const int kBlock = std::is_same<R, double>::value ? h.block64 : h.block32;
     const long long stride = (long long)h.G * h.ne * h.Nw;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = h.h_level_offsets[l];

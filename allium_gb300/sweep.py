@@ -143,6 +143,10 @@ class InverseAdvectionOperator:
         """0: one launch per wavefront level (default); 1: one persistent dataflow launch per sweep."""
         check(_lib.lib().allium_sweep_set_schedule(self.h, int(mode)), self.h)
 
+    def SetBlockSize(self, precision, threads):
+        """Threads per block (32/64/128) of the FP64 (64) or FP32 (32) level kernels."""
+        check(_lib.lib().allium_sweep_set_block_size(self.h, int(precision), int(threads)), self.h)
+
     def SetFactorCache(self, mode):
         """1: keep FP64 local-matrix inverses across Mults when memory allows (default); 0: off."""
         check(_lib.lib().allium_sweep_set_factor_cache(self.h, int(mode)), self.h)

@@ -153,6 +153,11 @@ int allium_sweep_set_schedule(allium_sweep* s, int mode);
  * when sigma_t > 0).  Meant as the inner operator of an FP64 outer iteration. */
 int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi);
 
+/* Threads per block (32, 64 or 128) of the thread-per-node level kernels of
+ * the FP64 (precision 64) or FP32 (32) sweeps; the autotuner's knob (no
+ * reference counterpart).  Default 128. */
+int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads);
+
 /* Negative-flux fixup inside the sweep (SetFixupOperator / UseFixup,
  * src/sweep.hpp:108-117, applied at src/sweep.cpp:465-470): kind 0 off,
  * 1 ZeroFixupOperator, 2 ZeroAndScaleFixupOperator (src/fixup.cpp:3-57),

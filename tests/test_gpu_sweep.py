@@ -477,3 +477,25 @@ def test_reflective_errors():
     with pytest.raises(AlliumError) as e:
         InverseAdvectionOperator(mesh, 1, quad, sig, bc={2: "reflective", 4: "reflective"})
     assert e.value.status == 2
+
+
+def test_autotune_keeps_results():
+    # every launch configuration computes each node with the same arithmetic
+    from allium_gb300.autotune import autotune
+    mesh, quad, sig = problem(3, (8, 8, 8), 1, sn=6, jitter=0.1, seed=3)
+    L = InverseAdvectionOperator(mesh, 1, quad, sig)
+    src = torch.rand(L.width, dtype=torch.float64, device="cuda")
+    a = torch.empty_like(src)
+    L.Mult(src, a)
+    f = torch.empty(L.width, dtype=torch.float32, device="cuda")
+    L.ToNodeLayoutF32(src, f)
+    fa = torch.empty_like(f)
+    L.MultF32Nodes(f, fa)
+    res = autotune(L, reps=2)
+    assert res["fp64"]["block"] in (32, 64, 128) and len(res["trials"]) >= 4
+    b = torch.empty_like(src)
+    L.Mult(src, b)
+    fb = torch.empty_like(f)
+    L.MultF32Nodes(f, fb)
+    L.synchronize()
+    assert torch.equal(a, b) and torch.equal(fa, fb)
