@@ -81,6 +81,10 @@ EXPORTS = {
     "allium_sweep_dsa_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_dsa_jacobi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_dsa_blocks": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "allium_sweep_neighbours": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "allium_pair_aggregates": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_csr_spmv": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                  C.c_double, C.c_void_p]),
     "allium_mlp_gemm": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_longlong, C.c_void_p,
                                   C.c_longlong, C.c_longlong, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p,
                                   C.c_float, C.c_float, C.c_int, C.c_void_p]),

@@ -778,6 +778,17 @@ int allium_sweep_dsa_jacobi(allium_sweep* s, const double* x, double* y) {
     return ALLIUM_OK;
 }
 
+int allium_sweep_neighbours(allium_sweep* s, int* out) {
+    if (!s || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    std::vector<allium::Slot> slots((size_t)h.ne * h.nface);
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(slots.data(), h.d_slots, slots.size() * sizeof(allium::Slot), cudaMemcpyDeviceToHost,
+                                    h.stream));
+    CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+    for (size_t i = 0; i < slots.size(); ++i) out[i] = slots[i].nbr >= 0 ? slots[i].nbr : -1;
+    return ALLIUM_OK;
+}
+
 int allium_sweep_dsa_blocks(allium_sweep* s, double* out) {
     if (!s || !out) return ALLIUM_ERR_ARG;
     Handle& h = s->h;

@@ -226,6 +226,18 @@ __global__ void k_dsa_invert(int ne, int G, int n, int nface, const double* __re
         for (int j = 0; j < n; ++j) out[i * n + j] = b[i][j];
 }
 
+// y = alpha A x + beta y for a CSR matrix (the coarse levels of the diffusion
+// preconditioner), one thread per row
+__global__ void k_csr_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                           const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y,
+                           double alpha, double beta) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double acc = 0.0;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) acc += val[k] * x[col[k]];
+    y[r] = beta == 0.0 ? alpha * acc : alpha * acc + beta * y[r];
+}
+
 }  // namespace
 
 bool dsa_supported(const Handle& h) { return h.n <= kDsaMaxN && h.lump == 0; }
@@ -261,3 +273,35 @@ cudaError_t launch_dsa_apply(Handle& h, const double* x, double* y) {
 }
 
 }  // namespace allium
+
+extern "C" int allium_csr_spmv(int n, const int* rowptr, const int* col, const double* val, const double* x, double* y,
+                               double alpha, double beta, void* stream) {
+    if (n <= 0 || !rowptr || !col || !val || !x || !y) return ALLIUM_ERR_ARG;
+    allium::k_csr_spmv<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(n, rowptr, col, val, x, y, alpha,
+                                                                                       beta);
+    return cudaGetLastError() == cudaSuccess ? ALLIUM_OK : ALLIUM_ERR_CUDA;
+}
+
+// Greedy pairwise aggregation of a CSR matrix (host arrays): rows in order,
+// an unaggregated row joins the unaggregated neighbour with the most negative
+// coupling (lowest column on ties), or stays alone.  agg[i] receives the
+// aggregate of row i; returns the number of aggregates.
+extern "C" int allium_pair_aggregates(int n, const int* rowptr, const int* col, const double* val, int* agg) {
+    if (n <= 0 || !rowptr || !col || !val || !agg) return -1;
+    for (int i = 0; i < n; ++i) agg[i] = -1;
+    int nagg = 0;
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        int best = -1;
+        double bv = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            const int j = col[k];
+            if (j == i || agg[j] >= 0) continue;
+            if (val[k] < bv || (val[k] == bv && best >= 0 && j < best)) { bv = val[k]; best = j; }
+        }
+        agg[i] = nagg;
+        if (best >= 0) agg[best] = nagg;
+        ++nagg;
+    }
+    return nagg;
+}

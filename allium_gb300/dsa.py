@@ -1,10 +1,11 @@
 """Diffusion synthetic acceleration with the GPU MIP diffusion operator.
 
 MIPDiffusion wraps the C ABI's MIP operator K (InteriorPenaltyDiscretization,
-src/moment_discretization.cpp:73-110) and solves K x = b with block-Jacobi
-preconditioned conjugate gradients (allium applies CG with BoomerAMG;
-BoomerAMG is a hypre library component, replaced here by the inverted cell
-blocks K_ee).  DSAPreconditioner is DiffusionSyntheticAccelerationOperator
+src/moment_discretization.cpp:73-110) and solves K x = b by preconditioned
+conjugate gradients: allium applies CG with hypre's BoomerAMG; here the
+preconditioner is AggregationVCycle (block-Jacobi smoothing on the DG level,
+the cellwise-constant Galerkin operator and pairwise aggregates below it) or
+plain block-Jacobi (the inverted cell blocks K_ee).  DSAPreconditioner is DiffusionSyntheticAccelerationOperator
 (src/transport_op.hpp:38-59): y = x + K^{-1} (M_s x), M_s the within-group
 scattering mass, for source iteration and as the right preconditioner of GMRES
 on T phi = phi - D L^{-1} D^T M_s phi.
@@ -42,6 +43,16 @@ class MIPDiffusion:
         check(_lib.lib().allium_sweep_dsa_apply(self.L.h, _p(x), _p(y)), self.L.h)
         return y
 
+    def use_vcycle(self, on=True, **kw):
+        """Precondition the diffusion CG with AggregationVCycle instead of block-Jacobi."""
+        self.vcycle = AggregationVCycle(self, **kw) if on else None
+
+    def _prec(self, r):
+        if getattr(self, "vcycle", None) is not None:
+            return self.vcycle(r)
+        z = torch.empty_like(r)
+        return self.jacobi(r, z)
+
     def jacobi(self, x, y):
         check(_lib.lib().allium_sweep_dsa_jacobi(self.L.h, _p(x), _p(y)), self.L.h)
         return y
@@ -63,11 +74,11 @@ class MIPDiffusion:
         return y
 
     def solve(self, b, tol=1e-10, maxiter=200):
-        """Block-Jacobi PCG on K x = b (x = 0 start); returns x."""
+        """PCG on K x = b (x = 0 start) with the V-cycle when one is set
+        (use_vcycle), block-Jacobi otherwise; returns x."""
         x = torch.zeros_like(b)
         r = b.clone()
-        z = torch.empty_like(b)
-        self.jacobi(r, z)
+        z = self._prec(r)
         p = z.clone()
         q = torch.empty_like(b)
         rz = torch.dot(r, z)
@@ -83,7 +94,7 @@ class MIPDiffusion:
             it += 1
             if torch.linalg.norm(r).item() <= tol * bn:
                 break
-            self.jacobi(r, z)
+            z = self._prec(r)
             rz_new = torch.dot(r, z)
             p.mul_(rz_new / rz).add_(z)
             rz = rz_new
@@ -94,8 +105,10 @@ class MIPDiffusion:
 class DSAPreconditioner:
     """y = x + K^{-1} M_s x (DiffusionSyntheticAccelerationOperator::Mult)."""
 
-    def __init__(self, Linv, sigma_s, cg_tol=1e-10, cg_maxiter=200, **kw):
+    def __init__(self, Linv, sigma_s, cg_tol=1e-10, cg_maxiter=200, vcycle=True, **kw):
         self.K = MIPDiffusion(Linv, sigma_s, **kw)
+        if vcycle:
+            self.K.use_vcycle()
         self.cg_tol, self.cg_maxiter = cg_tol, cg_maxiter
         self.tmp = None
         self.applications = 0
@@ -108,3 +121,168 @@ class DSAPreconditioner:
         torch.add(x, d, out=out)
         self.applications += 1
         return out
+
+
+def _csr_spmv(rowptr, col, val, x, y, alpha=1.0, beta=0.0):
+    _lib.lib().allium_csr_spmv(int(rowptr.numel() - 1), _p(rowptr), _p(col), _p(val), _p(x), _p(y), float(alpha),
+                               float(beta), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return y
+
+
+def _pair_aggregates(A):
+    """Two rounds of greedy pairwise aggregation (allium_pair_aggregates):
+    aggregates of up to four rows; returns (aggregate of every row, count)."""
+    import scipy.sparse as sp
+    L = _lib.lib()
+
+    def once(M):
+        M = M.tocsr()
+        M.sort_indices()
+        rp = np.ascontiguousarray(M.indptr, dtype=np.int32)
+        cl = np.ascontiguousarray(M.indices, dtype=np.int32)
+        vl = np.ascontiguousarray(M.data, dtype=np.float64)
+        agg = np.empty(M.shape[0], dtype=np.int32)
+        nagg = L.allium_pair_aggregates(M.shape[0], rp.ctypes.data, cl.ctypes.data, vl.ctypes.data, agg.ctypes.data)
+        return agg.astype(np.int64), nagg
+
+    a1, n1 = once(A)
+    P1 = sp.csr_matrix((np.ones(A.shape[0]), (np.arange(A.shape[0]), a1)), shape=(A.shape[0], n1))
+    a2, n2 = once(P1.T @ A @ P1)
+    return a2[a1], n2
+
+
+def _gll_nodes(p):
+    """Gauss-Lobatto nodes on [0, 1] (the sweep's L2 basis nodes), p <= 3."""
+    if p == 0:
+        return np.array([0.5])
+    if p == 1:
+        return np.array([0.0, 1.0])
+    if p == 2:
+        return np.array([0.0, 0.5, 1.0])
+    r = 1.0 / np.sqrt(5.0)
+    return np.array([0.0, 0.5 * (1 - r), 0.5 * (1 + r), 1.0])
+
+
+def _vertex_prolongation(mesh, order, G):
+    """P: continuous multilinear vertex values -> DG nodal values, for G
+    independent groups (rows g * Ndof + e * n + i, columns g * Nv + v)."""
+    import scipy.sparse as sp
+    dim = mesh.dim
+    corner_to_mfem = {1: [0, 1], 2: [0, 1, 3, 2], 3: [0, 1, 3, 2, 4, 5, 7, 6]}[dim]
+    x = _gll_nodes(order)
+    n1 = order + 1
+    n = n1 ** dim
+    ne, nv = mesh.num_elements, mesh.num_vertices
+    # corner shape functions at the DG nodes: W[i][c]
+    W = np.empty((n, 1 << dim))
+    for i in range(n):
+        idx = [(i // n1 ** d) % n1 for d in range(dim)]
+        for c in range(1 << dim):
+            w = 1.0
+            for d in range(dim):
+                t = x[idx[d]]
+                w *= t if (c >> d) & 1 else 1.0 - t
+            W[i, c] = w
+    verts = mesh.elements[:, corner_to_mfem]                      # [Ne][corners]
+    rows = (np.arange(ne)[:, None, None] * n + np.arange(n)[None, :, None]).repeat(1 << dim, axis=2)
+    cols = np.broadcast_to(verts[:, None, :], rows.shape)
+    vals = np.broadcast_to(W[None, :, :], rows.shape)
+    keep = vals != 0.0
+    P1 = sp.csr_matrix((vals[keep], (rows[keep], cols[keep])), shape=(ne * n, nv))
+    return sp.block_diag([P1] * G, format="csr")
+
+
+def _device_csr(M, dev):
+    M = M.tocsr()
+    M.sort_indices()
+    return (torch.from_numpy(M.indptr.astype(np.int32)).to(dev), torch.from_numpy(M.indices.astype(np.int32)).to(dev),
+            torch.from_numpy(M.data.astype(np.float64)).to(dev), M.shape[0])
+
+
+class AggregationVCycle:
+    """Symmetric V-cycle preconditioner for K, standing in for BoomerAMG:
+    damped block-Jacobi smoothing on the DG level; below it the continuous
+    multilinear (vertex) space, K_v = P^T K P with P the interpolation of
+    vertex values at the DG nodes; below that smoothed aggregation (aggregates
+    of up to four strongly coupled vertices, Jacobi-smoothed tentative
+    prolongator, damped Jacobi smoothing) down to a dense solve.  Built on the
+    host from K's blocks once per operator, applied on the device."""
+
+    def __init__(self, mip, omega0=0.7, omega=0.67, coarse=400):
+        import scipy.sparse as sp
+        self.mip, self.omega0, self.omega = mip, omega0, omega
+        L = mip.L
+        G, ne, n, nd = mip.G, L.mesh.num_elements, mip.n, 2 * L.dim
+        nbr = np.empty(ne * nd, dtype=np.int32)
+        check(_lib.lib().allium_sweep_neighbours(L.h, nbr.ctypes.data), L.h)
+        nbr = nbr.reshape(ne, nd)
+        B = mip.blocks()                                         # [G][Ne][1 + nd][n][n]
+        rows, cols, vals = [], [], []
+        ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        for g in range(G):
+            base = g * ne * n
+            e = np.arange(ne)[:, None, None]
+            rows.append((base + e * n + ii).ravel())
+            cols.append((base + e * n + jj).ravel())
+            vals.append(B[g, :, 0].ravel())
+            for k in range(nd):
+                m = np.nonzero(nbr[:, k] >= 0)[0]
+                em = m[:, None, None]
+                rows.append((base + em * n + ii).ravel())
+                cols.append((base + nbr[m, k][:, None, None] * n + jj).ravel())
+                vals.append(B[g, m, 1 + k].ravel())
+        K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                          shape=(G * ne * n, G * ne * n))
+        Pv = _vertex_prolongation(L.mesh, L.order, G)
+        dev = torch.device("cuda")
+        self.P0, self.R0 = _device_csr(Pv, dev), _device_csr(Pv.T, dev)
+        A = (Pv.T @ K @ Pv).tocsr()
+        self.levels = []
+        while True:
+            lvl = {"A": _device_csr(A, dev), "dinv": torch.from_numpy(1.0 / A.diagonal()).to(dev), "n": A.shape[0]}
+            self.levels.append(lvl)
+            if A.shape[0] <= coarse:
+                lvl["inv"] = torch.from_numpy(np.linalg.inv(A.toarray())).to(dev)
+                break
+            agg, nagg = _pair_aggregates(A)
+            T = sp.csr_matrix((np.ones(A.shape[0]), (np.arange(A.shape[0]), agg)), shape=(A.shape[0], nagg))
+            Dinv = sp.diags(1.0 / A.diagonal())
+            lam = float(np.max(np.asarray(abs(Dinv @ A).sum(axis=1)).ravel()))
+            P = (T - (4.0 / 3.0 / lam) * (Dinv @ (A @ T))).tocsr()
+            lvl["P"], lvl["R"] = _device_csr(P, dev), _device_csr(P.T, dev)
+            A = (P.T @ A @ P).tocsr()
+
+    @staticmethod
+    def _mv(M, x, out=None, alpha=1.0, beta=0.0):
+        rp, cl, vl, nrows = M
+        if out is None:
+            out = torch.empty(nrows, dtype=x.dtype, device=x.device)
+        return _csr_spmv(rp, cl, vl, x, out, alpha, beta)
+
+    def _scalar(self, l, r):
+        lvl = self.levels[l]
+        if "inv" in lvl:
+            return torch.mv(lvl["inv"], r)
+        x = self.omega * lvl["dinv"] * r
+        res = r.clone()
+        self._mv(lvl["A"], x, res, -1.0, 1.0)
+        x += self._mv(lvl["P"], self._scalar(l + 1, self._mv(lvl["R"], res)))
+        res.copy_(r)
+        self._mv(lvl["A"], x, res, -1.0, 1.0)
+        x += self.omega * lvl["dinv"] * res
+        return x
+
+    def __call__(self, r):
+        K = self.mip
+        z = torch.empty_like(r)
+        K.jacobi(r, z)
+        x = self.omega0 * z
+        res = torch.empty_like(r)
+        K.apply(x, res)
+        res = r - res
+        x += self._mv(self.P0, self._scalar(0, self._mv(self.R0, res)))
+        K.apply(x, res)
+        res = r - res
+        K.jacobi(res, z)
+        x += self.omega0 * z
+        return x

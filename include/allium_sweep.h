@@ -326,6 +326,21 @@ int allium_sweep_dsa_apply(allium_sweep* s, const double* x, double* y);
  * diffusion solve (no reference counterpart: allium uses BoomerAMG). */
 int allium_sweep_dsa_jacobi(allium_sweep* s, const double* x, double* y);
 
+/* y = alpha A x + beta y for a CSR matrix on the device (row pointers,
+ * column indices, values): the coarse levels of the diffusion
+ * preconditioner.  stream is a cudaStream_t (NULL: default stream). */
+int allium_csr_spmv(int n, const int* rowptr, const int* col, const double* val, const double* x, double* y,
+                    double alpha, double beta, void* stream);
+
+/* Greedy pairwise aggregation of a CSR matrix on the host (coarsening of the
+ * diffusion preconditioner): agg[i] = aggregate of row i; returns the number
+ * of aggregates (-1 on bad arguments). */
+int allium_pair_aggregates(int n, const int* rowptr, const int* col, const double* val, int* agg);
+
+/* Neighbour element across each local face, [Ne][2 dim] host ints, -1 on the
+ * boundary (the element-to-face table of src/sweep.cpp:123-135, resolved). */
+int allium_sweep_neighbours(allium_sweep* s, int* out);
+
 /* Copy K's blocks [G][Ne][1 + 2 dim][n][n] (self block, then the coupling to
  * the neighbour across each local face) to out (host or device). */
 int allium_sweep_dsa_blocks(allium_sweep* s, double* out);
