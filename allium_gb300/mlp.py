@@ -165,11 +165,15 @@ def face_neighbours(mesh):
 class LearnedInitialIterate:
     """Per-cell MLP predicting the next step's moments of a LinearizedTRT.
 
-    Input of cell e (standardised): log10 of the cell-mean moment of every
-    group, log10 sigma_g, log10 of the face neighbours' mean moment per group,
-    log10 of the cell-mean temperature and the temperature's nodal shape
-    T_i / T_mean - 1.  Output: the change of every (group, DOF) moment over the
-    step divided by the group's largest moment magnitude (standardised)."""
+    The prediction is the linear extrapolation phi_n + (phi_n - phi_{n-1})
+    plus a learned correction.  Input of cell e (standardised): log10 of the
+    cell-mean moment of every group, the cell-mean last change of every group
+    over the group's largest moment, log10 sigma_g, log10 of the face
+    neighbours' mean moment per group, log10 of the cell-mean temperature and
+    the temperature's nodal shape T_i / T_mean - 1.  Output: the deviation of
+    every (group, DOF) moment from the extrapolation over the group's largest
+    moment magnitude (standardised).  The network's last layer starts small,
+    so an untrained network returns about the extrapolation."""
 
     def __init__(self, trt, width=256, layers=4, seed=0, lr=1e-3):
         self.trt = trt
@@ -177,37 +181,52 @@ class LearnedInitialIterate:
         nb = face_neighbours(trt.L.mesh)
         dev = trt.T.device
         self.nb = torch.from_numpy(np.where(nb < 0, np.arange(self.ne)[:, None], nb)).to(dev)
-        self.nin = 3 * self.G + 1 + self.n
+        self.nin = 4 * self.G + 1 + self.n
         self.nout = self.G * self.n
         self.net = CellMLP(self.nin, self.nout, width=width, layers=layers, seed=seed, lr=lr, device=dev)
+        self.net.W[-1].mul_(0.01)
+        self.net.Wb[-1] = self.net.W[-1].to(torch.bfloat16)
         self.X, self.Y = [], []
         self.stats = None
         self.losses = []
+        self.last = None        # moments before the previous step
 
     def _scale(self, phi):
         return phi.view(self.G, -1).abs().amax(dim=1).clamp(min=1e-300)
 
-    def features(self, phi, T, sigma):
+    def _step_change(self, phi):
+        return phi - self.last if self.last is not None else torch.zeros_like(phi)
+
+    def features(self, phi, dphi, T, sigma):
         G, ne, n = self.G, self.ne, self.n
         pm = phi.view(G, ne, n).mean(dim=2)                          # [G][Ne]
         lp = torch.log10(pm.abs().clamp(min=1e-300))
+        dm = dphi.view(G, ne, n).mean(dim=2) / self._scale(phi).view(G, 1)
         ls = torch.log10(sigma.view(G, ne).clamp(min=1e-300))
         nbm = pm[:, self.nb].mean(dim=2)                              # [G][Ne]
         ln = torch.log10(nbm.abs().clamp(min=1e-300))
         Tc = T.view(ne, n)
         Tm = Tc.mean(dim=1, keepdim=True)
         shape = Tc / Tm.clamp(min=1e-300) - 1.0
-        X = torch.cat([lp.t(), ls.t(), ln.t(), torch.log10(Tm.clamp(min=1e-300)), shape], dim=1)
+        X = torch.cat([lp.t(), dm.t(), ls.t(), ln.t(), torch.log10(Tm.clamp(min=1e-300)), shape], dim=1)
         return X.float()
 
-    def target(self, phi_old, phi_new):
-        s = self._scale(phi_old)
-        d = (phi_new - phi_old).view(self.G, self.ne, self.n) / s.view(self.G, 1, 1)
+    def target(self, base, phi_new, scale):
+        d = (phi_new - base).view(self.G, self.ne, self.n) / scale.view(self.G, 1, 1)
         return d.permute(1, 0, 2).reshape(self.ne, self.G * self.n).float()
 
     def record(self, phi_old, T_old, sigma_old, phi_new):
-        self.X.append(self.features(phi_old, T_old, sigma_old))
-        self.Y.append(self.target(phi_old, phi_new))
+        """A training pair: state before a step -> moments after it."""
+        d = self._step_change(phi_old)
+        self.X.append(self.features(phi_old, d, T_old, sigma_old))
+        self.Y.append(self.target(phi_old + d, phi_new, self._scale(phi_old)))
+        self.last = phi_old.clone()
+
+    def extrapolate(self, phi):
+        """phi_n + (phi_n - phi_{n-1}), the prediction without the network."""
+        d = self._step_change(phi)
+        self.last = phi.clone()
+        return phi + d
 
     def train(self, epochs=20):
         X = torch.cat(self.X)
@@ -227,7 +246,9 @@ class LearnedInitialIterate:
 
     def predict(self, phi, T, sigma):
         mx, sx, my, sy = self.stats
-        Y = self.net.forward(((self.features(phi, T, sigma) - mx) / sx).contiguous()) * sy + my
-        d = Y.view(self.ne, self.G, self.n).permute(1, 0, 2).reshape(-1).double()
+        d = self._step_change(phi)
+        Y = self.net.forward(((self.features(phi, d, T, sigma) - mx) / sx).contiguous()) * sy + my
+        corr = Y.view(self.ne, self.G, self.n).permute(1, 0, 2).reshape(-1).double()
         s = self._scale(phi)
-        return phi + d * s.repeat_interleave(self.ne * self.n)
+        self.last = phi.clone()
+        return phi + d + corr * s.repeat_interleave(self.ne * self.n)
