@@ -60,7 +60,7 @@ def random_problems(count=256, seed=20261203, sides=(16, 256), orders=(1, 2, 3),
 class ProblemGroup:
     """Problems with one (order, S_N) in one union handle."""
 
-    def __init__(self, problems, cg_tol=1e-4, cg_maxiter=100):
+    def __init__(self, problems, cg_tol=1e-4, cg_maxiter=100, vcycle=True):
         self.problems = problems
         p0 = problems[0]
         self.order, self.sn = p0.order, p0.sn
@@ -80,7 +80,7 @@ class ProblemGroup:
         self.pid = torch.from_numpy(np.repeat(np.arange(len(problems)), counts)).to(dev)
         self.q = torch.from_numpy(FormTransportSource(self.L, qc)).to(dev)
         self.op = SchurOperator(self.L, ss)
-        self.dsa = DSAPreconditioner(self.L, ss, cg_tol=cg_tol, cg_maxiter=cg_maxiter)
+        self.dsa = DSAPreconditioner(self.L, ss, cg_tol=cg_tol, cg_maxiter=cg_maxiter, vcycle=vcycle)
         self.entries = self.L.width
 
     def norms(self, v):

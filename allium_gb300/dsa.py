@@ -105,7 +105,7 @@ class MIPDiffusion:
 class DSAPreconditioner:
     """y = x + K^{-1} M_s x (DiffusionSyntheticAccelerationOperator::Mult)."""
 
-    def __init__(self, Linv, sigma_s, cg_tol=1e-10, cg_maxiter=200, vcycle=True, **kw):
+    def __init__(self, Linv, sigma_s, cg_tol=1e-10, cg_maxiter=200, vcycle=False, **kw):
         self.K = MIPDiffusion(Linv, sigma_s, **kw)
         if vcycle:
             self.K.use_vcycle()
@@ -163,17 +163,11 @@ def _gll_nodes(p):
     return np.array([0.0, 0.5 * (1 - r), 0.5 * (1 + r), 1.0])
 
 
-def _vertex_prolongation(mesh, order, G):
-    """P: continuous multilinear vertex values -> DG nodal values, for G
-    independent groups (rows g * Ndof + e * n + i, columns g * Nv + v)."""
-    import scipy.sparse as sp
-    dim = mesh.dim
-    corner_to_mfem = {1: [0, 1], 2: [0, 1, 3, 2], 3: [0, 1, 3, 2, 4, 5, 7, 6]}[dim]
+def _corner_weights(dim, order):
+    """W[i][c]: multilinear corner shape c at DG node i (lexicographic nodes)."""
     x = _gll_nodes(order)
     n1 = order + 1
     n = n1 ** dim
-    ne, nv = mesh.num_elements, mesh.num_vertices
-    # corner shape functions at the DG nodes: W[i][c]
     W = np.empty((n, 1 << dim))
     for i in range(n):
         idx = [(i // n1 ** d) % n1 for d in range(dim)]
@@ -183,7 +177,21 @@ def _vertex_prolongation(mesh, order, G):
                 t = x[idx[d]]
                 w *= t if (c >> d) & 1 else 1.0 - t
             W[i, c] = w
-    verts = mesh.elements[:, corner_to_mfem]                      # [Ne][corners]
+    return W
+
+
+_CORNER_TO_MFEM = {1: [0, 1], 2: [0, 1, 3, 2], 3: [0, 1, 3, 2, 4, 5, 7, 6]}
+
+
+def _vertex_prolongation(mesh, order, G):
+    """P: continuous multilinear vertex values -> DG nodal values, for G
+    independent groups (rows g * Ndof + e * n + i, columns g * Nv + v)."""
+    import scipy.sparse as sp
+    dim = mesh.dim
+    W = _corner_weights(dim, order)
+    n = W.shape[0]
+    ne, nv = mesh.num_elements, mesh.num_vertices
+    verts = mesh.elements[:, _CORNER_TO_MFEM[dim]]                 # [Ne][corners]
     rows = (np.arange(ne)[:, None, None] * n + np.arange(n)[None, :, None]).repeat(1 << dim, axis=2)
     cols = np.broadcast_to(verts[:, None, :], rows.shape)
     vals = np.broadcast_to(W[None, :, :], rows.shape)
@@ -216,27 +224,36 @@ class AggregationVCycle:
         nbr = np.empty(ne * nd, dtype=np.int32)
         check(_lib.lib().allium_sweep_neighbours(L.h, nbr.ctypes.data), L.h)
         nbr = nbr.reshape(ne, nd)
-        B = mip.blocks()                                         # [G][Ne][1 + nd][n][n]
-        rows, cols, vals = [], [], []
-        ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
-        for g in range(G):
-            base = g * ne * n
-            e = np.arange(ne)[:, None, None]
-            rows.append((base + e * n + ii).ravel())
-            cols.append((base + e * n + jj).ravel())
-            vals.append(B[g, :, 0].ravel())
-            for k in range(nd):
-                m = np.nonzero(nbr[:, k] >= 0)[0]
-                em = m[:, None, None]
-                rows.append((base + em * n + ii).ravel())
-                cols.append((base + nbr[m, k][:, None, None] * n + jj).ravel())
-                vals.append(B[g, m, 1 + k].ravel())
-        K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
-                          shape=(G * ne * n, G * ne * n))
-        Pv = _vertex_prolongation(L.mesh, L.order, G)
         dev = torch.device("cuda")
+        # K_v = P^T K P from K's blocks on the device: every block B (self or
+        # face neighbour) contributes W^T B W between the two cells' vertices
+        W = torch.from_numpy(_corner_weights(L.dim, L.order)).to(dev)
+        nc = W.shape[1]
+        nv = L.mesh.num_vertices
+        B = torch.empty((G, ne, 1 + nd, n, n), dtype=torch.float64, device=dev)
+        check(_lib.lib().allium_sweep_dsa_blocks(L.h, _p(B)), L.h)
+        Cb = torch.einsum("ia,gesij,jb->gesab", W, B, W)            # [G][Ne][1+nd][nc][nc]
+        del B
+        verts = torch.from_numpy(L.mesh.elements[:, _CORNER_TO_MFEM[L.dim]].astype(np.int64)).to(dev)
+        other = torch.from_numpy(np.concatenate([np.arange(ne)[:, None], nbr], axis=1).astype(np.int64)).to(dev)
+        valid = other >= 0                                           # [Ne][1+nd]
+        rv = verts[:, None, :, None].expand(ne, 1 + nd, nc, nc)
+        cv = verts[other.clamp(min=0)][:, :, None, :].expand(ne, 1 + nd, nc, nc)
+        m = valid[:, :, None, None].expand(ne, 1 + nd, nc, nc)
+        rows_l, cols_l, vals_l = [], [], []
+        for g in range(G):
+            rows_l.append(rv[m] + g * nv)
+            cols_l.append(cv[m] + g * nv)
+            vals_l.append(Cb[g][m])
+        del Cb
+        keys = torch.cat(rows_l) * (G * nv) + torch.cat(cols_l)
+        vals = torch.cat(vals_l)
+        uk, inv = torch.unique(keys, return_inverse=True)
+        acc = torch.zeros(uk.numel(), dtype=torch.float64, device=dev).index_add_(0, inv, vals)
+        uk = uk.cpu().numpy()
+        A = sp.csr_matrix((acc.cpu().numpy(), (uk // (G * nv), uk % (G * nv))), shape=(G * nv, G * nv))
+        Pv = _vertex_prolongation(L.mesh, L.order, G)
         self.P0, self.R0 = _device_csr(Pv, dev), _device_csr(Pv.T, dev)
-        A = (Pv.T @ K @ Pv).tocsr()
         self.levels = []
         while True:
             lvl = {"A": _device_csr(A, dev), "dinv": torch.from_numpy(1.0 / A.diagonal()).to(dev), "n": A.shape[0]}

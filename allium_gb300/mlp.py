@@ -189,6 +189,7 @@ class LearnedInitialIterate:
         self.X, self.Y = [], []
         self.stats = None
         self.losses = []
+        self.gain = 1.0
         self.last = None        # moments before the previous step
 
     def _scale(self, phi):
@@ -228,9 +229,13 @@ class LearnedInitialIterate:
         self.last = phi.clone()
         return phi + d
 
-    def train(self, epochs=20):
-        X = torch.cat(self.X)
-        Y = torch.cat(self.Y)
+    def train(self, epochs=20, holdout=0.1):
+        """Train on all but the last `holdout` fraction of the recorded steps;
+        on those later steps fit the gain in [0, 1] applied to the network's
+        correction (0 when the correction does not beat the extrapolation)."""
+        nval = max(1, int(round(holdout * len(self.X)))) if len(self.X) > 1 else 0
+        X = torch.cat(self.X[:len(self.X) - nval])
+        Y = torch.cat(self.Y[:len(self.Y) - nval])
         mx, sx = X.mean(0), X.std(0).clamp(min=1e-6)
         my, sy = Y.mean(0), Y.std(0).clamp(min=1e-12)
         self.stats = (mx, sx, my, sy)
@@ -242,13 +247,21 @@ class LearnedInitialIterate:
             for k in range(0, Xn.shape[0] - B + 1, B):
                 idx = order[k:k + B]
                 self.losses.append(self.net.train_step(Xn[idx].contiguous(), Yn[idx].contiguous()))
+        self.gain = 1.0
+        if nval:
+            Xv = torch.cat(self.X[len(self.X) - nval:])
+            Yv = torch.cat(self.Y[len(self.Y) - nval:]).double()
+            pv = (self.net.forward(((Xv - mx) / sx).contiguous()) * sy + my).double()
+            den = torch.dot(pv.reshape(-1), pv.reshape(-1)).item()
+            a = torch.dot(Yv.reshape(-1), pv.reshape(-1)).item() / den if den > 0 else 0.0
+            self.gain = min(1.0, max(0.0, a))
         return float(self.losses[-1].item()) if self.losses else None
 
     def predict(self, phi, T, sigma):
         mx, sx, my, sy = self.stats
         d = self._step_change(phi)
         Y = self.net.forward(((self.features(phi, d, T, sigma) - mx) / sx).contiguous()) * sy + my
-        corr = Y.view(self.ne, self.G, self.n).permute(1, 0, 2).reshape(-1).double()
+        corr = self.gain * Y.view(self.ne, self.G, self.n).permute(1, 0, 2).reshape(-1).double()
         s = self._scale(phi)
         self.last = phi.clone()
         return phi + d + corr * s.repeat_interleave(self.ne * self.n)

@@ -198,7 +198,7 @@ def solve_section(L, mesh, quad, sigma, src, maxiter=400):
     # MIP-DSA as the right preconditioner of both (inexact block-Jacobi CG inside)
     from allium_gb300.dsa import DSAPreconditioner
     t0 = time.perf_counter()
-    dsa = DSAPreconditioner(L, sigma_s, cg_tol=1e-4, cg_maxiter=50)
+    dsa = DSAPreconditioner(L, sigma_s, cg_tol=1e-4, cg_maxiter=50, vcycle=False)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
     op3 = SchurOperator(L, sigma_s)
@@ -309,6 +309,7 @@ def learned_section(steps=200, train_steps=50, epochs=20):
     for k in runs:
         out[k] = {"krylov_iterations": its[k], "seconds": secs[k]}
     out["learned"]["train_seconds"] = train_s
+    out["learned"]["correction_gain"] = li.gain
     out["learned"]["samples"] = sum(x.shape[0] for x in li.X)
     out["iteration_ratio_vs_plain"] = its["plain"] / max(its["learned"], 1)
     out["iteration_ratio_vs_extrapolated"] = its["extrapolated"] / max(its["learned"], 1)
@@ -378,7 +379,7 @@ def chive2d_section(cpu=True):
     res = source_iteration(SchurOperator(L, sig_s), src, tol=1e-8)
     out = {"gpu_si": {"seconds": res.seconds, "iterations": res.iterations, "converged": res.converged}}
     t0 = time.perf_counter()
-    dsa = DSAPreconditioner(L, sig_s, cg_tol=1e-10, cg_maxiter=200)
+    dsa = DSAPreconditioner(L, sig_s, cg_tol=1e-10, cg_maxiter=200, vcycle=True)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
     acc = source_iteration(SchurOperator(L, sig_s), src, tol=1e-8, dsa=dsa)
