@@ -30,6 +30,7 @@ struct GemmArgs {
     const float* bias;        // [N] or null
     float alpha, beta;
     int relu;
+    int ksplit;               // > 1: blockIdx.z takes one of ksplit K ranges, C accumulated atomically
 };
 
 __device__ inline uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
@@ -51,18 +52,22 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g) {
 #pragma unroll
             for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.0f;
     const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    // K range of this block (whole K unless split)
+    const int kchunk = ((g.K + g.ksplit - 1) / g.ksplit + TK - 1) / TK * TK;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(g.K, kbeg + kchunk);
 
-    for (int k0 = 0; k0 < g.K; k0 += TK) {
+    for (int k0 = kbeg; k0 < kend; k0 += TK) {
         // stage A (64 x 32) and B (32 x 64), zero outside the matrices
         for (int idx = threadIdx.x; idx < TM * TK; idx += blockDim.x) {
             const int r = idx / TK, c = idx % TK;
             const int m = m0 + r, k = k0 + c;
-            As[r][c] = (m < g.M && k < g.K) ? g.A[(long long)m * g.sam + (long long)k * g.sak] : zero;
+            As[r][c] = (m < g.M && k < kend) ? g.A[(long long)m * g.sam + (long long)k * g.sak] : zero;
         }
         for (int idx = threadIdx.x; idx < TK * TN; idx += blockDim.x) {
             const int r = idx / TN, c = idx % TN;
             const int k = k0 + r, n = n0 + c;
-            Bs[r][c] = (k < g.K && n < g.N) ? g.B[(long long)k * g.sbk + (long long)n * g.sbn] : zero;
+            Bs[r][c] = (k < kend && n < g.N) ? g.B[(long long)k * g.sbk + (long long)n * g.sbn] : zero;
         }
         __syncthreads();
 #pragma unroll
@@ -108,6 +113,10 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g) {
                 const int n = n0 + wn + b * 8 + tig * 2 + (c & 1);
                 if (m >= g.M || n >= g.N) continue;
                 const long long o = (long long)m * g.ldc + n;
+                if (g.ksplit > 1) {   // partial sum of one K range (C zeroed beforehand)
+                    atomicAdd(g.C + o, g.alpha * acc[a][b][c]);
+                    continue;
+                }
                 float v = g.alpha * acc[a][b][c];
                 if (g.beta != 0.0f && g.C) v += g.beta * g.C[o];
                 if (g.bias) v += g.bias[n];
@@ -206,8 +215,19 @@ int allium_mlp_gemm(int M, int N, int K, const void* A, long long sam, long long
     g.B = static_cast<const __nv_bfloat16*>(B); g.sbk = sbk; g.sbn = sbn;
     g.C = C; g.ldc = ldc; g.Cb = static_cast<__nv_bfloat16*>(C_bf16); g.bias = bias;
     g.alpha = alpha; g.beta = beta; g.relu = relu;
-    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
-    k_gemm_bf16<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(g);
+    g.ksplit = 1;
+    const int tiles = ((N + TN - 1) / TN) * ((M + TM - 1) / TM);
+    // few output tiles over a long K (the weight gradients X^T dY over a batch):
+    // split K across blocks so the GPU fills, partial sums added atomically
+    if (tiles < 304 && K >= 8 * TK && C && !C_bf16 && !bias && !relu && beta == 0.0f && ldc == N) {
+        g.ksplit = (304 + tiles - 1) / tiles;
+        if (g.ksplit > K / (4 * TK)) g.ksplit = K / (4 * TK);
+        if (g.ksplit < 1) g.ksplit = 1;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (g.ksplit > 1 && cudaMemsetAsync(C, 0, (size_t)M * N * sizeof(float), st) != cudaSuccess) return ALLIUM_ERR_CUDA;
+    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, g.ksplit);
+    k_gemm_bf16<<<grid, 128, 0, st>>>(g);
     return status_of(cudaGetLastError());
 }
 

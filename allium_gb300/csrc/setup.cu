@@ -616,21 +616,26 @@ __global__ void k_moments(int Nw, int G, int dim, long long ndof, const double* 
 __global__ void k_moments_transpose(int Nw, int G, int dim, long long ndof, const double* __restrict__ omega,
                                     double wsum, const double* __restrict__ phi, double* __restrict__ psi,
                                     int nmom, double alpha, int add) {
+    // one thread per (g, i): the isotropic term p0 / sum_w does not depend on
+    // the angle, so it is divided once and written to every angle (the writes
+    // of a warp are contiguous for each angle)
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)G * Nw * ndof) return;
+    if (t >= (long long)G * ndof) return;
     const long long s = t % ndof;
-    const long long r = t / ndof;
-    const int a = (int)(r % Nw), g = (int)(r / Nw);
-    double* p = psi + psi_index(ndof, Nw, g, a, s);
+    const int g = (int)(t / ndof);
     const double p0 = phi[s + ndof * g];
-    double v = add ? __dadd_rn(*p, __ddiv_rn(__dmul_rn(alpha, p0), wsum)) : __ddiv_rn(p0, wsum);
-    for (int m = 0; m + 1 < nmom; ++m) {
-        const double ph = phi[s + ndof * (g + (long long)G * (1 + m))];
-        const double om = omega[a * dim + m];
-        const double c = add ? __dmul_rn(__dmul_rn(__dmul_rn(alpha, 3.0), om), ph) : __dmul_rn(__dmul_rn(3.0, om), ph);
-        v = __dadd_rn(v, __ddiv_rn(c, wsum));
+    const double q0 = add ? __ddiv_rn(__dmul_rn(alpha, p0), wsum) : __ddiv_rn(p0, wsum);
+    for (int a = 0; a < Nw; ++a) {
+        double* p = psi + psi_index(ndof, Nw, g, a, s);
+        double v = add ? __dadd_rn(*p, q0) : q0;
+        for (int m = 0; m + 1 < nmom; ++m) {
+            const double ph = phi[s + ndof * (g + (long long)G * (1 + m))];
+            const double om = omega[a * dim + m];
+            const double c = add ? __dmul_rn(__dmul_rn(__dmul_rn(alpha, 3.0), om), ph) : __dmul_rn(__dmul_rn(3.0, om), ph);
+            v = __dadd_rn(v, __ddiv_rn(c, wsum));
+        }
+        *p = v;
     }
-    *p = v;
 }
 
 cudaError_t launch_moments(Handle& h, const double* psi, double* phi, int nmom) {
@@ -641,7 +646,7 @@ cudaError_t launch_moments(Handle& h, const double* psi, double* phi, int nmom) 
 }
 
 cudaError_t launch_moments_transpose(Handle& h, const double* phi, double* psi, int nmom, double alpha, int add) {
-    const long long total = (long long)h.G * h.Nw * h.ndof;
+    const long long total = (long long)h.G * h.ndof;
     const int b = 256;
     k_moments_transpose<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.Nw, h.G, h.dim, h.ndof, h.d_omega, h.wsum,
                                                                             phi, psi, nmom, alpha, add);

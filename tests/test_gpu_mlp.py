@@ -88,3 +88,18 @@ def test_learned_iterate_keeps_answers():
         assert r.converged
         err = torch.max(torch.abs(learn.T - plain.T)).item() / torch.max(plain.T).item()
         assert err < 1e-6
+
+
+@pytest.mark.parametrize("M,N,K,ta", [(37, 64, 5000, True), (133, 256, 16384, True), (64, 64, 300, False)])
+def test_gemm_split_k(M, N, K, ta):
+    # few output tiles over a long K: the kernel splits K over blocks and adds
+    # the partial sums atomically (the weight gradients X^T dY over a batch)
+    from allium_gb300.mlp import gemm
+    rng = np.random.default_rng(K)
+    A = rng.normal(size=(K, M) if ta else (M, K)).astype(np.float32)
+    B = rng.normal(size=(K, N)).astype(np.float32)
+    out = gemm(torch.from_numpy(A).cuda().to(torch.bfloat16), torch.from_numpy(B).cuda().to(torch.bfloat16),
+               transA=ta)
+    a = bf16(A).T if ta else bf16(A)
+    ref = a @ bf16(B)
+    assert np.max(np.abs(out.cpu().numpy() - ref)) <= 1e-5 * np.max(np.abs(ref))
