@@ -64,11 +64,16 @@ int check_status(Handle& h) {
 void free_all(Handle& h) {
     allium::drop_graphs(h);
     if (h.capture_stream) cudaStreamDestroy(h.capture_stream);
+    for (cudaEvent_t ev : h.chunk_events)
+        if (ev) cudaEventDestroy(ev);
+    for (cudaStream_t st : {h.copy_in, h.copy_out, h.comp2})
+        if (st) cudaStreamDestroy(st);
     void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
                     h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts,
-                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu, h.d_orient, h.d_dsa, h.d_dsa_inv};
+                    h.d_refl, h.d_feed, h.d_bounds, h.d_nu, h.d_orient, h.d_dsa, h.d_dsa_inv,
+                    h.d_chunk_nodes, h.d_chunk_pos};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -305,6 +310,64 @@ static void prepare_factor_cache(Handle& h) {
     allium::drop_graphs(h);
 }
 
+static bool pinned_host(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// Host buffers, page-locked: the directions are split into chunks that are
+// independent sweeps (no reflective coupling), and chunk c's copy in, sweep
+// and copy out are pipelined with the other chunks' (copy engines in both
+// directions, two compute streams), so the host link and the sweep overlap.
+static int mult_host_chunked(Handle& h, const double* source, double* psi) {
+    const int C = h.Nw >= 16 ? 8 : h.Nw / 2;
+    if (int st = allium::build_chunks(h, C)) return st;
+    const auto mk = [](cudaStream_t* st) {
+        return *st ? cudaSuccess : cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
+    };
+    CUDA_OR_FAIL(h, mk(&h.copy_in));
+    CUDA_OR_FAIL(h, mk(&h.copy_out));
+    CUDA_OR_FAIL(h, mk(&h.comp2));
+    if ((int)h.chunk_events.size() < 3 * C + 1) {
+        for (cudaEvent_t ev : h.chunk_events) cudaEventDestroy(ev);
+        h.chunk_events.assign(3 * C + 1, nullptr);
+        for (auto& ev : h.chunk_events) CUDA_OR_FAIL(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    CUDA_OR_FAIL(h, ensure(&h.d_stage, (size_t)h.psi_size));
+    CUDA_OR_FAIL(h, allium::ensure_factors(h));
+    cudaEvent_t* ev = h.chunk_events.data();
+    cudaEvent_t start = ev[3 * C];
+    CUDA_OR_FAIL(h, cudaEventRecord(start, h.stream));
+    CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.copy_in, start, 0));
+    CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.comp2, start, 0));
+    CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.copy_out, start, 0));
+    for (int c = 0; c < C; ++c) {
+        const int a0 = h.h_chunk_angle[c], a1 = h.h_chunk_angle[c + 1];
+        const size_t bytes = (size_t)(a1 - a0) * h.ndof * sizeof(double);
+        for (int g = 0; g < h.G; ++g) {
+            const size_t off = ((size_t)g * h.Nw + a0) * h.ndof;
+            CUDA_OR_FAIL(h, cudaMemcpyAsync(h.d_stage + off, source + off, bytes, cudaMemcpyHostToDevice, h.copy_in));
+        }
+        CUDA_OR_FAIL(h, cudaEventRecord(ev[3 * c], h.copy_in));
+        cudaStream_t cs = (c % 2 == 0) ? h.stream : h.comp2;
+        CUDA_OR_FAIL(h, cudaStreamWaitEvent(cs, ev[3 * c], 0));
+        CUDA_OR_FAIL(h, allium::launch_sweep_chunk(h, h.d_stage, c, cs));
+        CUDA_OR_FAIL(h, cudaEventRecord(ev[3 * c + 1], cs));
+        CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.copy_out, ev[3 * c + 1], 0));
+        for (int g = 0; g < h.G; ++g) {
+            const size_t off = ((size_t)g * h.Nw + a0) * h.ndof;
+            CUDA_OR_FAIL(h, cudaMemcpyAsync(psi + off, h.d_stage + off, bytes, cudaMemcpyDeviceToHost, h.copy_out));
+        }
+    }
+    CUDA_OR_FAIL(h, cudaEventRecord(ev[3 * C - 1], h.copy_out));
+    CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.stream, ev[3 * C - 1], 0));
+    return check_status(h);
+}
+
 int allium_sweep_mult(allium_sweep* s, const double* source, double* psi) {
     if (!s || !source || !psi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
@@ -315,6 +378,9 @@ int allium_sweep_mult(allium_sweep* s, const double* source, double* psi) {
         CUDA_OR_FAIL(h, allium::launch_sweep_fp64(h, source, psi));
         return ALLIUM_OK;
     }
+    if (!ds && !dp && h.d_inv && h.nrefl == 0 && h.fix_kind == 0 && h.schedule == 0 && h.Nw >= 4 &&
+        pinned_host(source) && pinned_host(psi))
+        return mult_host_chunked(h, source, psi);
     CUDA_OR_FAIL(h, ensure(&h.d_stage, (size_t)h.psi_size));
     const size_t bytes = (size_t)h.psi_size * sizeof(double);
     const double* src = source;

@@ -67,6 +67,18 @@ struct Handle {
     int* d_face_e1k1 = nullptr;      // [nfaces][2]
     uint8_t* d_nbrmap = nullptr;
     FaceOrient* d_orient = nullptr;   // [ne][2 dim]
+    // angle chunks of the host-buffer Mult (copy / sweep / copy pipeline):
+    // nodes of chunk c in (level, cell, angle) order, their positions in the
+    // full level order, offsets [nchunk][num_levels + 1]; copy streams, a
+    // second compute stream and events
+    int nchunk = 0;
+    std::vector<int> h_chunk_angle;   // [nchunk + 1] first angle of each chunk
+    int* d_chunk_nodes = nullptr;
+    int* d_chunk_pos = nullptr;
+    std::vector<int> h_chunk_offsets;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr, comp2 = nullptr;
+    std::vector<cudaEvent_t> chunk_events;   // [3 * nchunk + 1]
+
     // threads per block of the thread-per-node level kernels (FP64, FP32)
     int block64 = 128, block32 = 128;
     double *d_G = nullptr, *d_M = nullptr, *d_Mt = nullptr, *d_F = nullptr, *d_sigma = nullptr;
@@ -93,7 +105,7 @@ struct Handle {
         void* dst = nullptr;
         cudaGraphExec_t exec = nullptr;
     };
-    static constexpr int kGraphSlots = 8;
+    static constexpr int kGraphSlots = 24;
     GraphEntry graphs[kGraphSlots];
     int graph_next = 0;
     cudaStream_t capture_stream = nullptr;
@@ -133,10 +145,10 @@ struct Handle {
 // Launch `body(stream)` through a cached CUDA graph keyed by (kind, src, dst):
 // captured once on a private stream, replayed on h.stream afterwards.
 template <typename Body>
-cudaError_t run_graph(Handle& h, int kind, const void* src, void* dst, Body&& body) {
-    if (!h.use_graphs) return body(h.stream);
+cudaError_t run_graph_on(Handle& h, int kind, const void* src, void* dst, cudaStream_t stream, Body&& body) {
+    if (!h.use_graphs) return body(stream);
     for (auto& g : h.graphs)
-        if (g.exec && g.kind == kind && g.src == src && g.dst == dst) return cudaGraphLaunch(g.exec, h.stream);
+        if (g.exec && g.kind == kind && g.src == src && g.dst == dst) return cudaGraphLaunch(g.exec, stream);
     cudaError_t e = cudaSuccess;
     if (!h.capture_stream) {
         e = cudaStreamCreateWithFlags(&h.capture_stream, cudaStreamNonBlocking);
@@ -157,7 +169,12 @@ cudaError_t run_graph(Handle& h, int kind, const void* src, void* dst, Body&& bo
     h.graph_next = (h.graph_next + 1) % Handle::kGraphSlots;
     if (slot.exec) cudaGraphExecDestroy(slot.exec);
     slot.kind = kind; slot.src = src; slot.dst = dst; slot.exec = exec;
-    return cudaGraphLaunch(exec, h.stream);
+    return cudaGraphLaunch(exec, stream);
+}
+
+template <typename Body>
+cudaError_t run_graph(Handle& h, int kind, const void* src, void* dst, Body&& body) {
+    return run_graph_on(h, kind, src, dst, h.stream, body);
 }
 
 inline void drop_graphs(Handle& h) {
@@ -192,6 +209,8 @@ cudaError_t launch_face_normals(Handle& h);
 cudaError_t launch_face_dots(Handle& h);
 cudaError_t launch_assemble(Handle& h);
 int compute_reflections(Handle& h, const std::vector<int>& refl_faces);   // allium status
+int build_chunks(Handle& h, int nchunk);                                     // allium status
+cudaError_t launch_sweep_chunk(Handle& h, double* stage, int c, cudaStream_t stream);
 
 // thermal radiative transfer operators (trt.cu)
 bool trt_supported(const Handle& h);

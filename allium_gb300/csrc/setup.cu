@@ -503,6 +503,79 @@ int compute_levels(Handle& h) {
     return ALLIUM_OK;
 }
 
+// ------------------------------------------------------------ angle chunks
+// key of level-order position t: chunk(angle) * num_levels + level
+__global__ void k_chunk_keys(long long n, int Nw, int nchunk, int nlev, const int* __restrict__ level_nodes,
+                             const int* __restrict__ level, int* __restrict__ keys) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int node = level_nodes[t];
+    const int a = node % Nw;
+    const int c = (int)(((long long)a * nchunk) / Nw);
+    keys[t] = c * nlev + level[node];
+}
+
+__global__ void k_gather_nodes(long long n, const int* __restrict__ pos, const int* __restrict__ level_nodes,
+                               int* __restrict__ out) {
+    const long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < n) out[u] = level_nodes[pos[u]];
+}
+
+// Orders for the chunked host-buffer Mult: angles split into nchunk contiguous
+// blocks (angle a in chunk a * nchunk / Nw); within a chunk the nodes keep the
+// (level, cell, angle) order of the full sweep (stable sort on the key).
+int build_chunks(Handle& h, int nchunk) {
+    if (h.nchunk == nchunk) return ALLIUM_OK;
+    const long long N = (long long)h.ne * h.Nw;
+    const int L = h.num_levels;
+    if ((long long)nchunk * L >= 0x7fffffffLL) { h.last_error = "too many chunk levels"; return ALLIUM_ERR_SIZE; }
+    if (h.d_chunk_nodes) { cudaFree(h.d_chunk_nodes); h.d_chunk_nodes = nullptr; }
+    if (h.d_chunk_pos) { cudaFree(h.d_chunk_pos); h.d_chunk_pos = nullptr; }
+    int *d_keys = nullptr, *d_keys2 = nullptr, *d_vals = nullptr, *d_hist = nullptr;
+    void* tmp = nullptr;
+    const int b = 256;
+    const unsigned gN = (unsigned)((N + b - 1) / b);
+    CK(cudaMalloc(&d_keys, N * sizeof(int)));
+    CK(cudaMalloc(&d_keys2, N * sizeof(int)));
+    CK(cudaMalloc(&d_vals, N * sizeof(int)));
+    CK(cudaMalloc(&h.d_chunk_pos, N * sizeof(int)));
+    CK(cudaMalloc(&h.d_chunk_nodes, N * sizeof(int)));
+    k_chunk_keys<<<gN, b, 0, h.stream>>>(N, h.Nw, nchunk, L, h.d_level_nodes, h.d_level, d_keys);
+    CK(cudaGetLastError());
+    k_iota<<<gN, b, 0, h.stream>>>(d_vals, N);
+    CK(cudaGetLastError());
+    int end_bit = 1;
+    while ((1LL << end_bit) <= (long long)nchunk * L) ++end_bit;
+    size_t tmp_bytes = 0;
+    CK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, d_keys, d_keys2, d_vals, h.d_chunk_pos, (int)N, 0, end_bit,
+                                       h.stream));
+    CK(cudaMalloc(&tmp, tmp_bytes));
+    CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, d_keys, d_keys2, d_vals, h.d_chunk_pos, (int)N, 0, end_bit,
+                                       h.stream));
+    k_gather_nodes<<<gN, b, 0, h.stream>>>(N, h.d_chunk_pos, h.d_level_nodes, h.d_chunk_nodes);
+    CK(cudaGetLastError());
+    const int nkeys = nchunk * L;
+    CK(cudaMalloc(&d_hist, (size_t)nkeys * sizeof(int)));
+    CK(cudaMemsetAsync(d_hist, 0, (size_t)nkeys * sizeof(int), h.stream));
+    k_level_hist<<<gN, b, 0, h.stream>>>(d_keys, N, d_hist);
+    CK(cudaGetLastError());
+    std::vector<int> hist(nkeys);
+    CK(cudaMemcpyAsync(hist.data(), d_hist, (size_t)nkeys * sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    CK(cudaStreamSynchronize(h.stream));
+    h.h_chunk_offsets.assign((size_t)nchunk * (L + 1), 0);
+    int run = 0;
+    for (int c = 0; c < nchunk; ++c) {
+        int* o = h.h_chunk_offsets.data() + (size_t)c * (L + 1);
+        for (int l = 0; l < L; ++l) { o[l] = run; run += hist[(size_t)c * L + l]; }
+        o[L] = run;
+    }
+    h.h_chunk_angle.assign(nchunk + 1, 0);
+    for (int c = 0; c <= nchunk; ++c) h.h_chunk_angle[c] = (int)(((long long)c * h.Nw + nchunk - 1) / nchunk);
+    cudaFree(d_hist); cudaFree(tmp); cudaFree(d_vals); cudaFree(d_keys2); cudaFree(d_keys);
+    h.nchunk = nchunk;
+    return ALLIUM_OK;
+}
+
 // ------------------------------------------------------------ source
 // FormTransportSource (sweep.cpp:1135-1185) for a piecewise-constant isotropic
 // density and an isotropic inflow per boundary attribute:

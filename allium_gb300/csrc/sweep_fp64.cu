@@ -89,6 +89,26 @@ cudaError_t launch_sweep_fp64(Handle& h, const double* src, double* psi) {
     return run_graph(h, 1, src, psi, [&](cudaStream_t st) { return sweep_dispatch<double, true>(h, a, st); });
 }
 
+// One angle chunk of the FP64 sweep from stored inverses, in place on the
+// staging buffer, on `stream` (graph kinds 40 + c)
+cudaError_t launch_sweep_chunk(Handle& h, double* stage, int c, cudaStream_t stream) {
+    SweepArgs<double> a;
+    a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
+    a.omega = h.d_omega; a.dots = h.d_dots; a.slots = h.d_slots; a.nbrmap = h.d_nbrmap;
+    a.Gm = h.d_G; a.M = h.d_M; a.Mt = h.d_Mt; a.F = h.d_F; a.sigma = h.d_sigma;
+    a.tau = h.tau; a.td = h.time_dependent ? 1 : 0;
+    a.src = stage; a.psi = stage; a.status = h.d_status; a.refl = h.d_refl;
+    a.fix_kind = 0; a.fix_min = 0.0; a.fix_counts = nullptr;
+    return run_graph_on(h, 40 + c, stage, stage, stream, [&](cudaStream_t st) -> cudaError_t {
+        switch (h.dim) {
+            case 1: return sweep_chunk<1, 1>(h, a, c, st);
+            case 2: return sweep_chunk<2, 1>(h, a, c, st);
+            case 3: return sweep_chunk<3, 1>(h, a, c, st);
+            default: return cudaErrorNotSupported;
+        }
+    });
+}
+
 bool factor_cache_supported(const Handle& h) { return h.p == 1 && h.dim >= 1 && h.dim <= 3; }
 
 template <int D, int P>

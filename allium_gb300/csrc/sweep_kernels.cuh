@@ -595,7 +595,8 @@ __global__ void __launch_bounds__(128) k_factor_all(SweepArgs<double> s, const i
 template <int D, int P, typename R>
 __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, const int* __restrict__ nodes,
                                                             int count, const R* __restrict__ inv,
-                                                            long long stride, long long base) {
+                                                            long long stride, long long base,
+                                                            const int* __restrict__ pos) {
     constexpr int N = ipow(P + 1, D);
     constexpr int NFACE = 2 * D;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -616,7 +617,9 @@ __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, cons
     }
     R b[N];
     assemble_rhs<D, P, R>(s, e, a, g, dots, nbrs, b);
-    const R* in = inv + base + t;
+    // stored inverse of this (node, group): level-order position base + t, or,
+    // for the angle-chunk orders, the node's level-order position pos[ni]
+    const R* in = inv + (pos ? (long long)pos[ni] * s.G + g : base + t);
     R x[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {

@@ -60,7 +60,28 @@ cudaError_t sweep_levels_cached(Handle& h, const SweepArgs<R>& args, const R* in
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
         k_sweep_cached_level<D, P, R><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, inv, stride,
-                                                                   (long long)off * h.G);
+                                                                   (long long)off * h.G, nullptr);
+    }
+    return cudaGetLastError();
+}
+
+// One angle chunk of the sweep: the chunk's nodes in (level, cell, angle)
+// order (h.d_chunk_nodes), its own level ranges; the stored inverses found
+// through each node's position in the full level order.
+template <int D, int P>
+cudaError_t sweep_chunk(Handle& h, const SweepArgs<double>& args, int c, cudaStream_t stream) {
+    const int kBlock = h.block64;
+    const long long stride = (long long)h.G * h.ne * h.Nw;
+    const int* offs = h.h_chunk_offsets.data() + (size_t)c * (h.num_levels + 1);
+    for (int l = 0; l < h.num_levels; ++l) {
+        const int off = offs[l];
+        const int count = offs[l + 1] - off;
+        if (count == 0) continue;
+        const long long threads = (long long)count * h.G;
+        if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
+        const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
+        k_sweep_cached_level<D, P, double><<<grid, kBlock, 0, stream>>>(args, h.d_chunk_nodes + off, count, h.d_inv,
+                                                                        stride, 0, h.d_chunk_pos + off);
     }
     return cudaGetLastError();
 }

@@ -128,7 +128,10 @@ int allium_sweep_set_time_absorption(allium_sweep* s, double tau);
 
 /* InverseAdvectionOperator::Mult (src/sweep.cpp:259-669), FP64 throughout,
  * partially pivoted local LU.  source may equal psi (in-place Mult(psi, psi),
- * as transport_op.hpp:28 and chive.cpp:733 call it). */
+ * as transport_op.hpp:28 and chive.cpp:733 call it).  With page-locked host
+ * vectors (and the factor cache on, no reflective faces, no fixup) the
+ * directions are swept in 8 independent chunks whose host->device copy, sweep
+ * and device->host copy overlap those of the other chunks. */
 int allium_sweep_mult(allium_sweep* s, const double* source, double* psi);
 
 /* FP64 factor cache (no counterpart in the reference, which refactors every
