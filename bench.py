@@ -565,6 +565,12 @@ def run_gpu(args):
                     "ms_per_step": e2e_s * 1e3},
             "gpu_launches": args.steps * (L.num_levels if tuned["fp64"]["schedule"] == 0 else 2),
             "roofline": roof,
+            # the kernel's own bound: GB300's FP64 pipe (1.25 TFLOP/s nominal = 625 G DFMA/s);
+            # per (cell, angle) node of the p = 1 hex sweep: 64 DFMA for inv(A) b plus 20 per
+            # inflow face (F u and its scaling), 3 inflow faces on average
+            "fp64_pipe": {"achieved_gdfma_s": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9,
+                          "peak_gdfma_s": 625.0, "peak_kind": "nominal",
+                          "frac": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9 / 625.0},
             "fp64_uncached": {"value": N / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                               "note": "every Mult assembles and factors all local systems (pivoted LU), as the reference does"},
             "fp64_first_mult_ms": ms_first,
