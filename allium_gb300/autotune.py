@@ -26,15 +26,17 @@ def _time(fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def autotune(L, reps=3, blocks=(32, 64, 128), fp32=True):
+def autotune(L, reps=3, blocks=(32, 64, 128), fp32=True, schedules=None):
     """Pick (schedule, FP64 block) on FP64 Mults and the FP32 node-layout block
-    on FP32 Mults; returns {"fp64": {...}, "fp32": {...}, "trials": [...]}."""
+    on FP32 Mults; returns {"fp64": {...}, "fp32": {...}, "trials": [...]}.
+    schedules restricts the schedules tried (0 levels, 1 dataflow)."""
     dev = torch.device("cuda")
     src = torch.rand(L.width, dtype=torch.float64, device=dev)
     psi = torch.empty_like(src)
-    schedules = [0]
-    if L.order <= 1 and not getattr(L, "has_reflective", False):
-        schedules.append(1)
+    if schedules is None:
+        schedules = [0]
+        if L.order <= 1 and not getattr(L, "has_reflective", False):
+            schedules.append(1)
     trials = []
     best = None
     for sch in schedules:

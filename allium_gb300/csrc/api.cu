@@ -73,7 +73,7 @@ void free_all(Handle& h) {
                     h.d_level, h.d_level_nodes, h.d_status, h.d_stage, h.f_stage, h.d_scratch, h.d_inv,
                     h.d_sigma_s, h.d_flags, h.d_flow_words, h.d_tile_start, h.d_tile_count, h.d_fix_counts,
                     h.d_refl, h.d_feed, h.d_bounds, h.d_nu, h.d_orient, h.d_dsa, h.d_dsa_inv,
-                    h.d_chunk_nodes, h.d_chunk_pos};
+                    h.d_chunk_nodes, h.d_chunk_pos, h.f_inv_nodes};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
@@ -633,7 +633,11 @@ int allium_sweep_set_factor_cache(allium_sweep* s, int mode) {
         cudaFree(h.d_inv);
         h.d_inv = nullptr;
         h.inv_valid = false;
+        if (h.f_inv_nodes) cudaFree(h.f_inv_nodes);
+        h.f_inv_nodes = nullptr;
+        h.f_inv_valid = false;
     }
+    if (mode == 1) h.f_inv_failed = false;
     return ALLIUM_OK;
 }
 

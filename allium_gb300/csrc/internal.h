@@ -97,6 +97,11 @@ struct Handle {
     int factor_cache = 1;            // 0 off, 1 automatic
     double* d_inv = nullptr;
     bool inv_valid = false;
+    // FP32 copy of the stored inverses for the node-major FP32 sweep, one
+    // contiguous n x n block per (level-order node, group)
+    float* f_inv_nodes = nullptr;
+    bool f_inv_valid = false;
+    bool f_inv_failed = false;        // the copy did not fit: recompute instead
 
     // CUDA graphs of the per-level launch sequence, keyed by kind and vectors
     struct GraphEntry {

@@ -34,6 +34,48 @@ cudaError_t sweep_levels_nodes(Handle& h, const SweepArgs<float>& args, cudaStre
     return cudaGetLastError();
 }
 
+template <int D, int P>
+cudaError_t sweep_levels_nodes_cached(Handle& h, const SweepArgs<float>& args, cudaStream_t stream) {
+    const int kBlock = h.block32;
+    for (int l = 0; l < h.num_levels; ++l) {
+        const int off = h.h_level_offsets[l];
+        const int count = h.h_level_offsets[l + 1] - off;
+        if (count == 0) continue;
+        const long long threads = (long long)count * h.G;
+        if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
+        const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
+        k_sweep_nodes_cached<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, h.f_inv_nodes,
+                                                                (long long)off * h.G);
+    }
+    return cudaGetLastError();
+}
+
+// FP32 copy of the stored FP64 inverses (allocated on first use; if it does
+// not fit, the node-major sweep keeps rebuilding its local systems)
+static bool ensure_f32_inverses(Handle& h) {
+    if (!h.d_inv || h.f_inv_failed) return false;
+    if (ensure_factors(h) != cudaSuccess) return false;
+    if (h.f_inv_valid) return true;
+    const int NN = h.n * h.n;
+    const long long total = (long long)h.G * h.ne * h.Nw;
+    if (!h.f_inv_nodes) {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        const size_t need = (size_t)total * NN * sizeof(float);
+        if (need > free_b / 2 || cudaMalloc(&h.f_inv_nodes, need) != cudaSuccess) {
+            cudaGetLastError();
+            h.f_inv_nodes = nullptr;
+            h.f_inv_failed = true;
+            return false;
+        }
+    }
+    const long long work = total * NN;
+    k_inv_to_f32<<<(unsigned)((work + 255) / 256), 256, 0, h.stream>>>(total, NN, total, h.d_inv, h.f_inv_nodes);
+    if (cudaGetLastError() != cudaSuccess) return false;
+    h.f_inv_valid = true;
+    return true;
+}
+
 cudaError_t launch_sweep_nodes_f32(Handle& h, const float* src, float* psi) {
     if (h.nrefl) return cudaErrorNotSupported;   // node layout: inflow/vacuum boundaries only
     SweepArgs<float> a;
@@ -43,6 +85,16 @@ cudaError_t launch_sweep_nodes_f32(Handle& h, const float* src, float* psi) {
     a.tau = (float)h.tau; a.td = h.time_dependent ? 1 : 0;
     a.src = src; a.psi = psi; a.status = h.d_status; a.refl = h.d_refl;
     a.fix_kind = h.fix_kind; a.fix_min = (float)h.fix_min; a.fix_counts = h.d_fix_counts;
+    // with stored inverses (factor cache on) every schedule applies them
+    if (h.p == 1 && ensure_f32_inverses(h))
+        return run_graph(h, 6, src, psi, [&](cudaStream_t st) -> cudaError_t {
+            switch (h.dim) {
+                case 1: return sweep_levels_nodes_cached<1, 1>(h, a, st);
+                case 2: return sweep_levels_nodes_cached<2, 1>(h, a, st);
+                case 3: return sweep_levels_nodes_cached<3, 1>(h, a, st);
+                default: return cudaErrorNotSupported;
+            }
+        });
     if (h.schedule == 1) {
         cudaError_t e = prepare_flow(h);
         if (e != cudaSuccess) return e;

@@ -58,7 +58,10 @@ cudaError_t ensure_factors(Handle& h) {
         case 31: e = factor_all<3, 1>(h, a); break;
         default: e = cudaErrorNotSupported;
     }
-    if (e == cudaSuccess) h.inv_valid = true;
+    if (e == cudaSuccess) {
+        h.inv_valid = true;
+        h.f_inv_valid = false;   // the FP32 copy follows the FP64 inverses
+    }
     return e;
 }
 

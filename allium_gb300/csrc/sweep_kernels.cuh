@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(128) k_factor_all(SweepArgs<double> s, const i
 }
 
 // Sweep with the stored inverses: psi = inv(A) (q + upwind terms).
-template <int D, int P, typename R>
+template <int D, int P, typename R, bool POS = false>
 __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, const int* __restrict__ nodes,
                                                             int count, const R* __restrict__ inv,
                                                             long long stride, long long base,
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, cons
     assemble_rhs<D, P, R>(s, e, a, g, dots, nbrs, b);
     // stored inverse of this (node, group): level-order position base + t, or,
     // for the angle-chunk orders, the node's level-order position pos[ni]
-    const R* in = inv + (pos ? (long long)pos[ni] * s.G + g : base + t);
+    const R* in = inv + (POS ? (long long)pos[ni] * s.G + g : base + t);
     R x[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -691,6 +691,81 @@ __global__ void __launch_bounds__(128, 4) k_sweep_nodes(SweepArgs<float> s, cons
     }
     if (!solve_local<N, false>(A, b)) atomicOr(s.status, kErrSingular);
     store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), b);
+}
+
+// FP32 copy of the stored FP64 inverses, one contiguous n x n block per
+// (level-order node, group): out[t][k] = inv64[k * stride + t]
+static __global__ void k_inv_to_f32(long long total, int NN, long long stride, const double* __restrict__ inv64,
+                                    float* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total * NN) return;
+    const long long t = idx % total;
+    const int k = (int)(idx / total);
+    out[t * NN + k] = (float)inv64[(long long)k * stride + t];
+}
+
+// Node-major FP32 sweep from the stored FP32 inverses: right-hand side as in
+// k_sweep_nodes, then psi = inv(A) b with the node's inverse read as float4 rows.
+template <int D, int P>
+__global__ void __launch_bounds__(128) k_sweep_nodes_cached(SweepArgs<float> s, const int* __restrict__ nodes,
+                                                            int count, const float* __restrict__ inv,
+                                                            long long base) {
+    constexpr int N = ipow(P + 1, D);
+    constexpr int NF = ipow(P + 1, D - 1);
+    constexpr int NFACE = 2 * D;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count * s.G) return;
+    const int ni = t / s.G;
+    const int g = t - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+    float b[N];
+    load_block<N>(s.src + node_index(s.Nw, s.G, N, e, a, g), b);
+#pragma unroll
+    for (int k = 0; k < NFACE; ++k) {
+        const Slot q = s.slots[(size_t)e * NFACE + k];
+        const float d1 = s.dots[(size_t)q.face * s.Nw + a];
+        const float dk = q.side ? -d1 : d1;
+        if (dk < 0.0f && q.nbr >= 0) {
+            const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
+            float nb[N];
+            load_block<N>(s.psi + node_index(s.Nw, s.G, N, q.nbr, a, g), nb);
+            float u[NF];
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) {
+                const int m = map[jj];
+                float v = nb[0];
+#pragma unroll
+                for (int c = 1; c < N; ++c) v = (m == c) ? nb[c] : v;
+                u[jj] = v;
+            }
+            const float* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
+            const float rd = -dk;
+#pragma unroll
+            for (int ii = 0; ii < NF; ++ii) {
+                float frow[NF];
+                load_block<NF>(F + ii * NF, frow);
+                float acc = 0.0f;
+#pragma unroll
+                for (int jj = 0; jj < NF; ++jj) acc = fmaf(frow[jj], u[jj], acc);
+                const int fi = face_dof(D, P, k, ii);
+                b[fi] = fmaf(rd, acc, b[fi]);
+            }
+        }
+    }
+    const float* in = inv + (base + t) * (long long)(N * N);
+    float x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        float row[N];
+        load_block<N>(in + i * N, row);
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j < N; ++j) acc = fmaf(row[j], b[j], acc);
+        x[i] = acc;
+    }
+    store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), x);
 }
 
 // RIGHT (g, a, i) FP64 <-> node-major FP32, and the node-major scattering source / moments

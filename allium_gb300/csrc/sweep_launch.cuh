@@ -80,8 +80,8 @@ cudaError_t sweep_chunk(Handle& h, const SweepArgs<double>& args, int c, cudaStr
         const long long threads = (long long)count * h.G;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_cached_level<D, P, double><<<grid, kBlock, 0, stream>>>(args, h.d_chunk_nodes + off, count, h.d_inv,
-                                                                        stride, 0, h.d_chunk_pos + off);
+        k_sweep_cached_level<D, P, double, true><<<grid, kBlock, 0, stream>>>(args, h.d_chunk_nodes + off, count,
+                                                                              h.d_inv, stride, 0, h.d_chunk_pos + off);
     }
     return cudaGetLastError();
 }

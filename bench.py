@@ -489,7 +489,8 @@ def run_gpu(args):
     ms_first = max_over_ranks(_timed(stream, 1, lambda i: L.Mult(srcs[0], psi)))
     # launch configuration chosen by the autotuner (schedule, threads per block)
     from allium_gb300.autotune import autotune
-    tuned = autotune(L, reps=3)
+    tuned = autotune(L, reps=3, schedules=None if args.schedule == "auto" else
+                     ([0] if args.schedule == "levels" else [1]))
     for i in range(args.warmup):
         L.Mult(srcs[i % 2], psi)
     barrier()
@@ -581,11 +582,11 @@ def run_gpu(args):
             "fp32": {"value": N / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32,
                      "max_rel_err_vs_fp64": err32,
                      "roofline_frac": (8.0 * N / (ms32 * 1e-3) / 1e9) / peak,
-                     "note": "allium's RIGHT layout, from stored FP32 inverses"},
+                     "note": "allium's RIGHT layout, local systems rebuilt and solved in FP32 each sweep"},
             "fp32_nodes": {"value": N / (ms32n * 1e-3), "unit": UNIT, "ms_per_step": ms32n,
                            "max_rel_err_vs_fp64": err32n,
                            "roofline_frac": (8.0 * N / (ms32n * 1e-3) / 1e9) / peak,
-                           "note": "node-major layout, local systems rebuilt and solved in FP32 each sweep"},
+                           "note": "node-major layout (the refinement's inner sweep), from an FP32 copy of the stored inverses"},
             "clocks": clk.summary()}
     if not args.no_solve:
         line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0])
@@ -614,6 +615,9 @@ def main():
     ap.add_argument("--cells", type=int, default=CELLS[0], help="cells per axis (smaller cases for profiling)")
     ap.add_argument("--no-solve", action="store_true", help="skip the time-to-tolerance solves")
     ap.add_argument("--trt-steps", type=int, default=200, help="time steps of the multigroup TRT section")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "levels", "dataflow"],
+                    help="sweep schedule: chosen by the autotuner, or fixed (for profiler runs, whose "
+                         "serialised launches would skew the tuner)")
     ap.add_argument("--batch-problems", type=int, default=256, help="problems of the batched section (0 skips it)")
     args = ap.parse_args()
     if args.impl == "reference":
