@@ -69,8 +69,14 @@ static bool ensure_f32_inverses(Handle& h) {
             return false;
         }
     }
-    const long long work = total * NN;
-    k_inv_to_f32<<<(unsigned)((work + 255) / 256), 256, 0, h.stream>>>(total, NN, total, h.d_inv, h.f_inv_nodes);
+    const long long work = total * h.n;
+    const unsigned grid = (unsigned)((work + 255) / 256);
+    switch (h.n) {
+        case 2: k_inv_to_f32<2><<<grid, 256, 0, h.stream>>>(total, total, h.d_inv, h.f_inv_nodes); break;
+        case 4: k_inv_to_f32<4><<<grid, 256, 0, h.stream>>>(total, total, h.d_inv, h.f_inv_nodes); break;
+        case 8: k_inv_to_f32<8><<<grid, 256, 0, h.stream>>>(total, total, h.d_inv, h.f_inv_nodes); break;
+        default: return false;
+    }
     if (cudaGetLastError() != cudaSuccess) return false;
     h.f_inv_valid = true;
     return true;

@@ -694,14 +694,19 @@ __global__ void __launch_bounds__(128, 4) k_sweep_nodes(SweepArgs<float> s, cons
 }
 
 // FP32 copy of the stored FP64 inverses, one contiguous n x n block per
-// (level-order node, group): out[t][k] = inv64[k * stride + t]
-static __global__ void k_inv_to_f32(long long total, int NN, long long stride, const double* __restrict__ inv64,
-                                    float* __restrict__ out) {
+// (level-order node, group): out[t][i][j] = inv64[(i n + j) stride + t].  One
+// thread per (t, row i): reads coalesced across t, writes one contiguous row.
+template <int N>
+__global__ void k_inv_to_f32(long long total, long long stride, const double* __restrict__ inv64,
+                             float* __restrict__ out) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= total * NN) return;
+    if (idx >= total * N) return;
     const long long t = idx % total;
-    const int k = (int)(idx / total);
-    out[t * NN + k] = (float)inv64[(long long)k * stride + t];
+    const int i = (int)(idx / total);
+    float row[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) row[j] = (float)inv64[(long long)(i * N + j) * stride + t];
+    store_block<N>(out + (t * N + i) * N, row);
 }
 
 // Node-major FP32 sweep from the stored FP32 inverses: right-hand side as in

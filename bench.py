@@ -179,6 +179,8 @@ def solve_section(L, mesh, quad, sigma, src, maxiter=400):
     # operator setup shared by both: stored FP64 and FP32 local inverses
     f = src.float()
     L.MultF32(f, f)
+    L.ToNodeLayoutF32(src, f)      # the node-layout inner sweep's FP32 copy of the inverses
+    L.MultF32Nodes(f, f)
     torch.cuda.synchronize()
     del f
     out = {}
