@@ -33,7 +33,7 @@ import torch
 from . import _lib
 from ._lib import check
 from .solvers import SolveResult, gmres, refine_rhs
-from .sweep import DiscreteToMoment, FormTransportSource, InverseAdvectionOperator, MomentsF32
+from .sweep import DiscreteToMoment, FormTransportSource, InverseAdvectionOperator, MomentsF32, MomentsF32Nodes
 
 
 def log_spaced_groups(emin, emax, G):
@@ -134,12 +134,16 @@ class TRTSchurOperator:
         return out
 
     def apply32(self, x, out):
+        """The same operator with the FP32 sweep on the node-major layout
+        [cell][angle][group][DOF] (isotropic source broadcast over angles)."""
         s = self.s
         em = self._emission_of(x)
-        s.psi32.view(s.G, s.Nw, s.ndof).copy_((em.view(s.G, 1, s.ndof) / s.wsum).expand(s.G, s.Nw, s.ndof))
-        s.L.MultF32(s.psi32, s.psi32)
+        n = s.n
+        src = (em.view(s.G, s.ne, n) / s.wsum).permute(1, 0, 2)          # [Ne][G][n]
+        s.psi32.view(s.ne, s.Nw, s.G, n).copy_(src[:, None, :, :].expand(s.ne, s.Nw, s.G, n))
+        s.L.MultF32Nodes(s.psi32, s.psi32)
         self.sweeps32 += 1
-        MomentsF32(s.L, s.psi32, s.mom)
+        MomentsF32Nodes(s.L, s.psi32, s.mom)
         torch.sub(x, s.mom, out=out)
         return out
 
