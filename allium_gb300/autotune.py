@@ -3,7 +3,8 @@
 The knobs are the schedule (wavefront levels, one launch per level captured
 in a CUDA graph, or the persistent dataflow kernel with per-node completion
 flags) and the threads per block of the thread-per-node level kernels, for
-the FP64 sweep and the FP32 sweep (node-major layout) separately.  Each
+the FP64 sweep and the FP32 sweep (node-major layout) separately, and the
+shape of the pinned-host-buffer pipeline (direction slices, compute streams).  Each
 candidate is timed with CUDA events over a few Mults after one untimed call
 (which captures its graph and, for FP64, builds the factor cache once), the
 fastest is kept and set on the handle.  Every candidate computes each node
@@ -65,3 +66,26 @@ def autotune(L, reps=3, blocks=(32, 64, 128), fp32=True, schedules=None):
         out["fp32"] = best32
     L.synchronize()
     return out
+
+
+def autotune_pipeline(L, h_src, h_psi, reps=3, shapes=((8, 4), (8, 3), (8, 2), (4, 4), (16, 4), (6, 3))):
+    """Pick the (slices, compute streams) of the pinned-host-buffer Mult: each
+    shape is timed on the host clock (the call returns once psi is back in
+    host memory) after two untimed calls, median of `reps`; the fastest is set
+    on the handle.  Returns {"best": {...}, "trials": [...]}."""
+    import time
+    trials = []
+    for chunks, streams in shapes:
+        L.SetPipeline(chunks, streams)
+        L.Mult(h_src, h_psi)
+        L.Mult(h_src, h_psi)
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            L.Mult(h_src, h_psi)
+            ts.append(time.perf_counter() - t0)
+        ts.sort()
+        trials.append({"chunks": chunks, "streams": streams, "ms": 1e3 * ts[len(ts) // 2]})
+    best = min(trials, key=lambda t: t["ms"])
+    L.SetPipeline(best["chunks"], best["streams"])
+    return {"best": best, "trials": trials}

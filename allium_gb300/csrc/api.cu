@@ -66,7 +66,7 @@ void free_all(Handle& h) {
     if (h.capture_stream) cudaStreamDestroy(h.capture_stream);
     for (cudaEvent_t ev : h.chunk_events)
         if (ev) cudaEventDestroy(ev);
-    for (cudaStream_t st : {h.copy_in, h.copy_out, h.comp2})
+    for (cudaStream_t st : {h.copy_in, h.copy_out, h.comp[1], h.comp[2], h.comp[3]})
         if (st) cudaStreamDestroy(st);
     void* bufs[] = {h.d_omega, h.d_weights, h.d_corners, h.d_normals, h.d_dots, h.f_dots, h.d_slots, h.d_face_e1k1, h.d_nbrmap,
                     h.d_G, h.d_M, h.d_Mt, h.d_F, h.d_sigma, h.f_G, h.f_M, h.f_Mt, h.f_F, h.f_sigma,
@@ -118,7 +118,6 @@ int allium_sweep_create(const allium_mesh_desc* mesh, const allium_fe_desc* fe, 
     if (fe->order < 0 || fe->order > allium::kMaxOrder || fe->basis != ALLIUM_BASIS_GAUSS_LOBATTO ||
         fe->lump < 0 || fe->lump > 7)
         return ALLIUM_ERR_UNSUPPORTED;
-    if (mesh->dim == 3 && fe->order > 2) return ALLIUM_ERR_UNSUPPORTED;   // 64 x 64 local systems
     std::vector<int> refl_attrs;
     if (bc)
         for (int i = 0; i < bc->num; ++i) {
@@ -324,14 +323,15 @@ static bool pinned_host(const void* p) {
 // and copy out are pipelined with the other chunks' (copy engines in both
 // directions, two compute streams), so the host link and the sweep overlap.
 static int mult_host_chunked(Handle& h, const double* source, double* psi) {
-    const int C = h.Nw >= 16 ? 8 : h.Nw / 2;
+    const int C = h.pipe_chunks < h.Nw / 2 ? h.pipe_chunks : h.Nw / 2;
+    const int S = h.pipe_streams < C ? h.pipe_streams : C;
     if (int st = allium::build_chunks(h, C)) return st;
     const auto mk = [](cudaStream_t* st) {
         return *st ? cudaSuccess : cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
     };
     CUDA_OR_FAIL(h, mk(&h.copy_in));
     CUDA_OR_FAIL(h, mk(&h.copy_out));
-    CUDA_OR_FAIL(h, mk(&h.comp2));
+    for (int k = 1; k < S; ++k) CUDA_OR_FAIL(h, mk(&h.comp[k]));
     if ((int)h.chunk_events.size() < 3 * C + 1) {
         for (cudaEvent_t ev : h.chunk_events) cudaEventDestroy(ev);
         h.chunk_events.assign(3 * C + 1, nullptr);
@@ -343,8 +343,8 @@ static int mult_host_chunked(Handle& h, const double* source, double* psi) {
     cudaEvent_t start = ev[3 * C];
     CUDA_OR_FAIL(h, cudaEventRecord(start, h.stream));
     CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.copy_in, start, 0));
-    CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.comp2, start, 0));
     CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.copy_out, start, 0));
+    for (int k = 1; k < S; ++k) CUDA_OR_FAIL(h, cudaStreamWaitEvent(h.comp[k], start, 0));
     for (int c = 0; c < C; ++c) {
         const int a0 = h.h_chunk_angle[c], a1 = h.h_chunk_angle[c + 1];
         const size_t bytes = (size_t)(a1 - a0) * h.ndof * sizeof(double);
@@ -353,7 +353,7 @@ static int mult_host_chunked(Handle& h, const double* source, double* psi) {
             CUDA_OR_FAIL(h, cudaMemcpyAsync(h.d_stage + off, source + off, bytes, cudaMemcpyHostToDevice, h.copy_in));
         }
         CUDA_OR_FAIL(h, cudaEventRecord(ev[3 * c], h.copy_in));
-        cudaStream_t cs = (c % 2 == 0) ? h.stream : h.comp2;
+        cudaStream_t cs = (c % S == 0) ? h.stream : h.comp[c % S];
         CUDA_OR_FAIL(h, cudaStreamWaitEvent(cs, ev[3 * c], 0));
         CUDA_OR_FAIL(h, allium::launch_sweep_chunk(h, h.d_stage, c, cs));
         CUDA_OR_FAIL(h, cudaEventRecord(ev[3 * c + 1], cs));
@@ -480,6 +480,21 @@ int allium_sweep_moments(allium_sweep* s, const double* psi, double* phi, int nm
     if (e == cudaSuccess && (!dph || !dps)) e = cudaStreamSynchronize(h.stream);
     if (!dph) cudaFree(y);
     CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_relayout(allium_sweep* s, const double* in, int in_layout, double* out, int out_layout) {
+    if (!s || !in || !out) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    const auto known = [](int l) { return l == ALLIUM_LAYOUT_RIGHT || l == ALLIUM_LAYOUT_LEFT; };
+    if (!known(in_layout) || !known(out_layout)) { h.last_error = "unknown layout"; return ALLIUM_ERR_ARG; }
+    if (!on_device(in) || !on_device(out)) { h.last_error = "relayout takes device vectors"; return ALLIUM_ERR_ARG; }
+    const size_t bytes = (size_t)h.psi_size * sizeof(double);
+    const char* a = reinterpret_cast<const char*>(in);
+    const char* b = reinterpret_cast<const char*>(out);
+    if (a < b + bytes && b < a + bytes) { h.last_error = "relayout vectors overlap"; return ALLIUM_ERR_ARG; }
+    if (in_layout == out_layout) CUDA_OR_FAIL(h, cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, h.stream));
+    else CUDA_OR_FAIL(h, allium::launch_relayout(h, in, out, out_layout == ALLIUM_LAYOUT_LEFT));
     return ALLIUM_OK;
 }
 
@@ -668,6 +683,15 @@ int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads) {
         b = threads;
         allium::drop_graphs(h);
     }
+    return ALLIUM_OK;
+}
+
+int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams) {
+    if (!s || chunks < 2 || chunks > allium::Handle::kMaxPipeChunks || streams < 1 ||
+        streams > allium::Handle::kMaxPipeStreams)
+        return ALLIUM_ERR_ARG;
+    s->h.pipe_chunks = chunks;
+    s->h.pipe_streams = streams;
     return ALLIUM_OK;
 }
 

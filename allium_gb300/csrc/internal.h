@@ -69,14 +69,20 @@ struct Handle {
     FaceOrient* d_orient = nullptr;   // [ne][2 dim]
     // angle chunks of the host-buffer Mult (copy / sweep / copy pipeline):
     // nodes of chunk c in (level, cell, angle) order, their positions in the
-    // full level order, offsets [nchunk][num_levels + 1]; copy streams, a
-    // second compute stream and events
+    // full level order, offsets [nchunk][num_levels + 1]; copy streams,
+    // compute streams (comp[0] unused: h.stream) and events.  pipe_chunks
+    // and pipe_streams are the requested chunk count and compute streams.
+    static constexpr int kMaxPipeChunks = 32;
+    static constexpr int kMaxPipeStreams = 4;
+    int pipe_chunks = 8;
+    int pipe_streams = 4;
     int nchunk = 0;
     std::vector<int> h_chunk_angle;   // [nchunk + 1] first angle of each chunk
     int* d_chunk_nodes = nullptr;
     int* d_chunk_pos = nullptr;
     std::vector<int> h_chunk_offsets;
-    cudaStream_t copy_in = nullptr, copy_out = nullptr, comp2 = nullptr;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaStream_t comp[kMaxPipeStreams] = {};
     std::vector<cudaEvent_t> chunk_events;   // [3 * nchunk + 1]
 
     // threads per block of the thread-per-node level kernels (FP64, FP32)
@@ -110,7 +116,7 @@ struct Handle {
         void* dst = nullptr;
         cudaGraphExec_t exec = nullptr;
     };
-    static constexpr int kGraphSlots = 24;
+    static constexpr int kGraphSlots = 48;
     GraphEntry graphs[kGraphSlots];
     int graph_next = 0;
     cudaStream_t capture_stream = nullptr;
@@ -214,6 +220,7 @@ cudaError_t launch_face_normals(Handle& h);
 cudaError_t launch_face_dots(Handle& h);
 cudaError_t launch_assemble(Handle& h);
 int compute_reflections(Handle& h, const std::vector<int>& refl_faces);   // allium status
+cudaError_t launch_relayout(Handle& h, const double* in, double* out, int to_left);
 int build_chunks(Handle& h, int nchunk);                                     // allium status
 cudaError_t launch_sweep_chunk(Handle& h, double* stage, int c, cudaStream_t stream);
 

@@ -526,6 +526,9 @@ __global__ void k_gather_nodes(long long n, const int* __restrict__ pos, const i
 // (level, cell, angle) order of the full sweep (stable sort on the key).
 int build_chunks(Handle& h, int nchunk) {
     if (h.nchunk == nchunk) return ALLIUM_OK;
+    // the captured chunk sweeps (graph kinds 40 + c) hold the old chunk offsets
+    CK(cudaStreamSynchronize(h.stream));
+    drop_graphs(h);
     const long long N = (long long)h.ne * h.Nw;
     const int L = h.num_levels;
     if ((long long)nchunk * L >= 0x7fffffffLL) { h.last_error = "too many chunk levels"; return ALLIUM_ERR_SIZE; }
@@ -901,6 +904,52 @@ cudaError_t launch_scatter_source_f32(Handle& h, const double* sigma_s, const do
 __global__ void k_to_f32(const double* __restrict__ in, float* __restrict__ out, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (float)in[i];
+}
+
+// Transport-vector layouts (tvector.hpp:47-53): RIGHT psi(g,a,i) at
+// i + Ndof (a + Nw g), LEFT at g + G (a + Nw i).  With c = g + G a both are a
+// (c, i) matrix, row-major one way and column-major the other; one 32 x 32 tile
+// per block is staged in shared memory so reads and writes are both coalesced.
+__global__ void __launch_bounds__(256) k_relayout(long long ndof, int Nw, int G, const double* __restrict__ in,
+                                                  double* __restrict__ out, int to_left) {
+    __shared__ double tile[32][33];   // tile[c - c0][i - i0]
+    const long long i0 = (long long)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int GN = G * Nw;
+    if (to_left) {
+        for (int k = ty; k < 32; k += 8) {
+            const int c = c0 + k;
+            const long long i = i0 + tx;
+            if (c < GN && i < ndof) tile[k][tx] = in[i + ndof * ((c / G) + (long long)Nw * (c % G))];
+        }
+        __syncthreads();
+        for (int k = ty; k < 32; k += 8) {
+            const int c = c0 + tx;
+            const long long i = i0 + k;
+            if (c < GN && i < ndof) out[c + (long long)GN * i] = tile[tx][k];
+        }
+    } else {
+        for (int k = ty; k < 32; k += 8) {
+            const int c = c0 + tx;
+            const long long i = i0 + k;
+            if (c < GN && i < ndof) tile[tx][k] = in[c + (long long)GN * i];
+        }
+        __syncthreads();
+        for (int k = ty; k < 32; k += 8) {
+            const int c = c0 + k;
+            const long long i = i0 + tx;
+            if (c < GN && i < ndof) out[i + ndof * ((c / G) + (long long)Nw * (c % G))] = tile[k][tx];
+        }
+    }
+}
+
+cudaError_t launch_relayout(Handle& h, const double* in, double* out, int to_left) {
+    const long long tiles_i = (h.ndof + 31) / 32;
+    const long long tiles_c = ((long long)h.G * h.Nw + 31) / 32;
+    if (tiles_i > 0x7fffffffLL || tiles_c > 65535) return cudaErrorInvalidValue;
+    k_relayout<<<dim3((unsigned)tiles_i, (unsigned)tiles_c), 256, 0, h.stream>>>(h.ndof, h.Nw, h.G, in, out, to_left);
+    return cudaGetLastError();
 }
 
 static cudaError_t to_f32(Handle& h, const double* in, float** out, long long n) {

@@ -123,6 +123,15 @@ cudaError_t apply_L_launch(Handle& h, const ApplyArgs& a) {
     return cudaGetLastError();
 }
 
+template <int D, int P>
+cudaError_t apply_L_rows_launch(Handle& h, const ApplyArgs& a) {
+    constexpr int kBlock = 128;
+    const long long total = (long long)h.G * h.ne * h.Nw * ipow(P + 1, D);
+    const unsigned grid = (unsigned)((total + kBlock - 1) / kBlock);
+    k_apply_L_rows<D, P><<<grid, kBlock, 0, h.stream>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y) {
     ApplyArgs a;
     a.ne = h.ne; a.Nw = h.Nw; a.G = h.G; a.ndof = h.ndof;
@@ -142,6 +151,7 @@ cudaError_t launch_apply_L_fp64(Handle& h, const double* x, double* y) {
         case 30: return apply_L_launch<3, 0>(h, a);
         case 31: return apply_L_launch<3, 1>(h, a);
         case 32: return apply_L_launch<3, 2>(h, a);
+        case 33: return apply_L_rows_launch<3, 3>(h, a);
         default: return cudaErrorNotSupported;
     }
 }

@@ -566,6 +566,153 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
     if (act) s.psi[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)] = br;
 }
 
+// Block per (node, group) for local systems wider than a warp (3D p = 3:
+// 64 x 64, 33 KB in FP64).  The system sits in shared memory, one row per
+// thread, and is solved by Gaussian elimination with the team kernel's pivot
+// rule (largest magnitude, first row on ties) and arithmetic (reciprocal of the
+// pivot, multiplier A[i][k] * inv, back substitution by x_k = b_k * inv_k).
+template <int D, int P, typename R, bool PIVOT>
+__global__ void __launch_bounds__(64) k_sweep_block(SweepArgs<R> s, const int* __restrict__ nodes) {
+    constexpr int N1 = P + 1;
+    constexpr int N = ipow(N1, D);
+    constexpr int NF = ipow(N1, D - 1);
+    constexpr int NFACE = 2 * D;
+    constexpr int LD = N + 1;   // odd row stride: a column walk touches distinct banks
+    constexpr int NW = N / 32;
+    static_assert(N == 64, "block kernel is laid out for 64 x 64 local systems");
+    __shared__ R A[N * LD];
+    __shared__ R b[N];
+    __shared__ R wbest[NW];
+    __shared__ int widx[NW];
+    const int r = threadIdx.x;
+    const int lane = r & 31, warp = r >> 5;
+    const int ni = blockIdx.x / s.G;   // the grid is exactly count * G blocks
+    const int g = blockIdx.x - ni * s.G;
+    const int node = nodes[ni];
+    const int e = node / s.Nw;
+    const int a = node - e * s.Nw;
+
+    int rid[3] = {0, 0, 0};
+    {
+        int q = r;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { rid[d] = q % N1; q /= N1; }
+    }
+    R om[3] = {R(0), R(0), R(0)};
+#pragma unroll
+    for (int d = 0; d < D; ++d) om[d] = R(s.omega[a * D + d]);
+    {
+        const R* Gm = s.Gm + (size_t)e * D * N * N;
+        const R* M = s.M + (size_t)e * N * N;
+        const R* Mt = s.Mt + (size_t)e * N * N;
+        const R sg = s.sigma[(size_t)g * s.ne + e];
+        for (int idx = r; idx < N * N; idx += N) {
+            R v = om[0] * Gm[idx];
+#pragma unroll
+            for (int d = 1; d < D; ++d) v = fma_r(om[d], Gm[d * N * N + idx], v);
+            v = fma_r(sg, M[idx], v);
+            if (s.td) v = fma_r(s.tau, Mt[idx], v);
+            A[(idx / N) * LD + idx % N] = v;
+        }
+    }
+    R br = s.src[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)];
+    __syncthreads();
+
+    static_for<0, NFACE>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int ax = k / 2, side = k % 2;
+        const Slot q = s.slots[(size_t)e * NFACE + k];
+        const R d1 = s.dots[(size_t)q.face * s.Nw + a];
+        const R dk = q.side ? -d1 : d1;
+        const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
+        if (dk > R(0)) {   // outflow face: (Omega.n) F on the face block, one add per entry
+            for (int idx = r; idx < NF * NF; idx += N) {
+                const int ii = idx / NF, jj = idx - ii * NF;
+                R* dst = &A[face_dof(D, P, k, ii) * LD + face_dof(D, P, k, jj)];
+                *dst = fma_r(dk, F[idx], *dst);
+            }
+        }
+        const bool on = rid[ax] == side * P;
+        int ii = 0, stride = 1;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            if (d != ax) { ii += rid[d] * stride; stride *= N1; }
+        if (dk < R(0) && q.nbr >= 0 && on) {
+            const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
+            const R* up = s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)q.nbr * N);
+            R acc = R(0);
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) acc = fma_r(F[ii * NF + jj], up[map[jj]], acc);
+            br = fma_r(-dk, acc, br);
+        }
+        if (dk < R(0) && q.nbr <= -2 && on) {
+            const int ar = s.refl[(size_t)(-2 - q.nbr) * s.Nw + a];
+            const R* own = s.psi + psi_index(s.ndof, s.Nw, g, ar, (long long)e * N);
+            R acc = R(0);
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) acc = fma_r(F[ii * NF + jj], own[face_dof(D, P, k, jj)], acc);
+            br = fma_r(-dk, acc, br);
+        }
+        __syncthreads();   // faces share edge and corner entries: one face at a time
+    });
+    b[r] = br;
+    __syncthreads();
+
+    bool ok = true;
+    R myinv = R(0);
+    for (int k = 0; k < N; ++k) {
+        if (PIVOT) {
+            R best = (r >= k) ? R(fabs(A[r * LD + k])) : R(-1);
+            int bi = r;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const R ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) { wbest[warp] = best; widx[warp] = bi; }
+            __syncthreads();
+            best = wbest[0];
+            bi = widx[0];
+#pragma unroll
+            for (int w = 1; w < NW; ++w)
+                if (wbest[w] > best || (wbest[w] == best && widx[w] < bi)) { best = wbest[w]; bi = widx[w]; }
+            if (bi != k) {   // the same on every thread
+                if (r >= k) {
+                    const R t = A[k * LD + r];
+                    A[k * LD + r] = A[bi * LD + r];
+                    A[bi * LD + r] = t;
+                }
+                if (r == 0) {
+                    const R t = b[k];
+                    b[k] = b[bi];
+                    b[bi] = t;
+                }
+            }
+            __syncthreads();
+        }
+        const R akk = A[k * LD + k];
+        ok = ok && (akk != R(0));
+        const R inv = R(1) / akk;
+        if (r == k) myinv = inv;
+        if (r > k) {
+            const R l = A[r * LD + k] * inv;
+            for (int j = k + 1; j < N; ++j) A[r * LD + j] = fma_r(-l, A[k * LD + j], A[r * LD + j]);
+            b[r] = fma_r(-l, b[k], b[r]);
+        }
+        __syncthreads();
+    }
+    // back substitution; b[r] of rows below k is final once row k is reached
+    for (int k = N - 1; k >= 0; --k) {
+        if (r == k) b[k] = b[k] * myinv;
+        __syncthreads();
+        if (r < k) b[r] = fma_r(-A[r * LD + k], b[k], b[r]);
+    }
+    __syncthreads();
+    if (!ok && r == 0) atomicOr(s.status, kErrSingular);
+    s.psi[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)] = b[r];
+}
+
 // Inverse of every local matrix, in one pass over all node-groups of all levels
 // (no level ordering needed: the local matrices do not depend on upstream
 // data).  Node-group t of the level-sorted order is stored entry-major,
@@ -1119,6 +1266,79 @@ __global__ void __launch_bounds__(128) k_apply_L(ApplyArgs s) {
     double* ye = s.y + psi_index(s.ndof, s.Nw, g, a, (long long)e * N);
 #pragma unroll
     for (int i = 0; i < N; ++i) ye[i] = y[i];
+}
+
+// The same operator with one thread per row (3D p = 3: a thread per node would
+// hold 2 x 64 doubles).  Row i gets the sums of k_apply_L's row i, in its order.
+template <int D, int P>
+__global__ void __launch_bounds__(128) k_apply_L_rows(ApplyArgs s) {
+    constexpr int N1 = P + 1;
+    constexpr int N = ipow(N1, D);
+    constexpr int NF = ipow(N1, D - 1);
+    constexpr int NFACE = 2 * D;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)s.G * s.ne * s.Nw * N;
+    if (t >= total) return;
+    const int i = (int)(t % N);
+    const long long nd = t / N;
+    const int a = (int)(nd % s.Nw);
+    const long long r = nd / s.Nw;
+    const int e = (int)(r % s.ne);
+    const int g = (int)(r / s.ne);
+    int rid[3] = {0, 0, 0};
+    {
+        int q = i;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { rid[d] = q % N1; q /= N1; }
+    }
+    double om[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) om[d] = s.omega[a * D + d];
+    const double* xv = s.x + psi_index(s.ndof, s.Nw, g, a, (long long)e * N);
+    const double* Gm = s.Gm + (size_t)e * D * N * N;
+    const double* M = s.M + (size_t)e * N * N;
+    const double sg = s.sigma[(size_t)g * s.ne + e];
+    double m = 0.0, gr = 0.0, mt = 0.0;
+    for (int j = 0; j < N; ++j) {
+        const double xj = xv[j];
+        m = fma(M[i * N + j], xj, m);
+        double c = om[0] * Gm[i * N + j];
+#pragma unroll
+        for (int d = 1; d < D; ++d) c = fma(om[d], Gm[d * N * N + i * N + j], c);
+        gr = fma(c, xj, gr);
+    }
+    if (s.td) {
+        const double* Mt = s.Mt + (size_t)e * N * N;
+        for (int j = 0; j < N; ++j) mt = fma(Mt[i * N + j], xv[j], mt);
+    }
+    double y = fma(sg, m, fma(s.tau, mt, gr));
+#pragma unroll
+    for (int k = 0; k < NFACE; ++k) {
+        const int ax = k / 2, side = k % 2;
+        if (rid[ax] != side * P) continue;
+        int ii = 0, stride = 1;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            if (d != ax) { ii += rid[d] * stride; stride *= N1; }
+        const Slot q = s.slots[(size_t)e * NFACE + k];
+        const double d1 = s.dots[(size_t)q.face * s.Nw + a];
+        const double dk = q.side ? -d1 : d1;
+        const double* F = s.F + ((size_t)e * NFACE + k) * NF * NF + ii * NF;
+        if (dk > 0.0) {
+            double acc = 0.0;
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) acc = fma(F[jj], xv[face_dof(D, P, k, jj)], acc);
+            y = fma(dk, acc, y);
+        } else if (dk < 0.0 && q.nbr >= 0) {
+            const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
+            const double* up = s.x + psi_index(s.ndof, s.Nw, g, a, (long long)q.nbr * N);
+            double acc = 0.0;
+#pragma unroll
+            for (int jj = 0; jj < NF; ++jj) acc = fma(F[jj], up[map[jj]], acc);
+            y = fma(dk, acc, y);
+        }
+    }
+    s.y[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + i)] = y;
 }
 
 }  // namespace allium

@@ -38,6 +38,19 @@ cudaError_t sweep_levels_team(Handle& h, const SweepArgs<R>& args, cudaStream_t 
     return cudaGetLastError();
 }
 
+template <int D, int P, typename R, bool PIVOT>
+cudaError_t sweep_levels_block(Handle& h, const SweepArgs<R>& args, cudaStream_t stream) {
+    for (int l = 0; l < h.num_levels; ++l) {
+        const int off = h.h_level_offsets[l];
+        const int count = h.h_level_offsets[l + 1] - off;
+        if (count == 0) continue;
+        const long long blocks = (long long)count * h.G;
+        if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+        k_sweep_block<D, P, R, PIVOT><<<(unsigned)blocks, 64, 0, stream>>>(args, h.d_level_nodes + off);
+    }
+    return cudaGetLastError();
+}
+
 // All-node factor pass and the sweep from stored inverses (p = 1).
 template <int D, int P>
 cudaError_t factor_all(Handle& h, const SweepArgs<double>& args) {
@@ -143,7 +156,8 @@ cudaError_t flow_dispatch(Handle& h, const SweepArgs<R>& a, const R* inv, cudaSt
 
 // Thread per node while the local system fits a thread's registers (N <= 8):
 // fewest instructions per node, and every lane busy on the FP64 pipe.  Team
-// kernel (lane per row) for the larger systems, which would spill.
+// kernel (lane per row) for the larger systems, which would spill; block per
+// node (shared-memory system) for 3D p = 3, wider than a warp.
 template <typename R, bool PIVOT>
 cudaError_t sweep_dispatch(Handle& h, const SweepArgs<R>& a, cudaStream_t st) {
     switch (h.dim * 10 + h.p) {
@@ -158,6 +172,7 @@ cudaError_t sweep_dispatch(Handle& h, const SweepArgs<R>& a, cudaStream_t st) {
         case 30: return sweep_levels<3, 0, R, PIVOT>(h, a, st);
         case 31: return sweep_levels<3, 1, R, PIVOT>(h, a, st);
         case 32: return sweep_levels_team<3, 2, R, PIVOT>(h, a, st);
+        case 33: return sweep_levels_block<3, 3, R, PIVOT>(h, a, st);
         default: return cudaErrorNotSupported;
     }
 }

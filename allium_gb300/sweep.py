@@ -147,6 +147,10 @@ class InverseAdvectionOperator:
         """Threads per block (32/64/128) of the FP64 (64) or FP32 (32) level kernels."""
         check(_lib.lib().allium_sweep_set_block_size(self.h, int(precision), int(threads)), self.h)
 
+    def SetPipeline(self, chunks, streams):
+        """Direction slices (2..32) and compute streams (1..4) of the pinned-host-buffer Mult."""
+        check(_lib.lib().allium_sweep_set_pipeline(self.h, int(chunks), int(streams)), self.h)
+
     def SetFactorCache(self, mode):
         """1: keep FP64 local-matrix inverses across Mults when memory allows (default); 0: off."""
         check(_lib.lib().allium_sweep_set_factor_cache(self.h, int(mode)), self.h)
@@ -165,6 +169,17 @@ class InverseAdvectionOperator:
         check(_lib.lib().allium_sweep_from_node_layout_f32(self.h, C.c_void_p(_ptr(v, np.float32, self.width, "v")),
                                                            C.c_void_p(_ptr(psi, np.float64, self.width, "psi"))), self.h)
         return psi
+
+    RIGHT, LEFT = 0, 1
+
+    def Relayout(self, x, x_layout, out, out_layout):
+        """Copy a psi-sized float64 CUDA tensor between the RIGHT layout
+        (i + Ndof (a + Nw g), the one every other call takes) and the LEFT
+        layout (g + G (a + Nw i)) of src/tvector.hpp:47-53."""
+        check(_lib.lib().allium_sweep_relayout(self.h, C.c_void_p(_ptr(x, np.float64, self.width, "x")), int(x_layout),
+                                               C.c_void_p(_ptr(out, np.float64, self.width, "out")), int(out_layout)),
+              self.h)
+        return out
 
     def AssembleLocalMatrices(self, sigma_t=None):
         """Reassemble with new total cross sections [G, Ne] (numpy, or a float64

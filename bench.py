@@ -531,6 +531,8 @@ def run_gpu(args):
     # --- e2e through the C ABI with pinned host buffers (copies inside the timed region)
     h_srcs = [s.cpu().pin_memory() for s in srcs]
     h_psi = torch.empty_like(h_srcs[0]).pin_memory()
+    from allium_gb300.autotune import autotune_pipeline
+    pipe = autotune_pipeline(L, h_srcs[0], h_psi)   # untimed: picks the slices and compute streams
     L.Mult(h_srcs[0], h_psi)
     barrier()
     t0 = time.perf_counter()
@@ -565,7 +567,9 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(L.num_levels, cells),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
-                    "ms_per_step": e2e_s * 1e3},
+                    "ms_per_step": e2e_s * 1e3,
+                    "pipeline": {"chunks": pipe["best"]["chunks"], "compute_streams": pipe["best"]["streams"],
+                                 "trials_ms": {f"{t['chunks']}x{t['streams']}": round(t["ms"], 2) for t in pipe["trials"]}}},
             "gpu_launches": args.steps * (L.num_levels if tuned["fp64"]["schedule"] == 0 else 2),
             "roofline": roof,
             # the kernel's own bound: GB300's FP64 pipe (1.25 TFLOP/s nominal = 625 G DFMA/s);

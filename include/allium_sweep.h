@@ -49,6 +49,10 @@ enum allium_status {
 enum allium_bc_kind { ALLIUM_BC_INFLOW = 0, ALLIUM_BC_REFLECTIVE = 1 };  /* src/bdr_conditions.hpp:5-10 */
 enum allium_lump { ALLIUM_LUMP_MASS = 1, ALLIUM_LUMP_GRADIENT = 2, ALLIUM_LUMP_FACE = 4 };  /* src/lumping.hpp:10-18 */
 enum allium_basis { ALLIUM_BASIS_GAUSS_LOBATTO = 0 };
+/* Transport-vector layouts (src/tvector.hpp:47-55, chosen by the reference's
+ * TRANSPORT_VECTOR_LAYOUT build option, RIGHT by default):
+ * RIGHT psi(g,a,i) at i + Ndof (a + Nw g); LEFT at g + G (a + Nw i). */
+enum allium_layout { ALLIUM_LAYOUT_RIGHT = 0, ALLIUM_LAYOUT_LEFT = 1 };
 
 /* Mesh of segments (dim 1), quadrilaterals (dim 2) or hexahedra (dim 3) with
  * (multi)linear geometry.  element_vertices uses MFEM's local vertex order:
@@ -68,7 +72,7 @@ typedef struct {
     const int* boundary_attributes;     /* [num_boundary_faces] */
 } allium_mesh_desc;
 
-/* L2 DG space: order p in 0..3 (0..2 on hexahedra), Gauss-Lobatto basis, lumping bit mask
+/* L2 DG space: order p in 0..3, Gauss-Lobatto basis, lumping bit mask
  * (allium's `lump` constructor argument, src/sweep.hpp:83). */
 typedef struct {
     int order;
@@ -161,6 +165,15 @@ int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi);
  * reference counterpart).  Default 128. */
 int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads);
 
+/* Shape of the host-buffer pipeline of allium_sweep_mult (pinned host vectors,
+ * stored inverses, inflow boundaries): the directions are cut into `chunks`
+ * contiguous slices (2..32, at most half the directions), each copied in,
+ * swept and copied out on its own, and the sweeps of consecutive slices
+ * alternate over `streams` compute streams (1..4).  Default 8 and 4.  No
+ * reference counterpart (the reference's vectors are host memory).  Results
+ * do not depend on either knob. */
+int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams);
+
 /* Negative-flux fixup inside the sweep (SetFixupOperator / UseFixup,
  * src/sweep.hpp:108-117, applied at src/sweep.cpp:465-470): kind 0 off,
  * 1 ZeroFixupOperator, 2 ZeroAndScaleFixupOperator (src/fixup.cpp:3-57),
@@ -198,6 +211,12 @@ int allium_sweep_balance_noalloc(allium_sweep* s, const double* psi, double* out
 
 /* DiscreteToMoment::Mult (src/transport_op.cpp:3-31); num_moments is 1 or dim+1. */
 int allium_sweep_moments(allium_sweep* s, const double* psi, double* phi, int num_moments);
+
+/* Copy a psi-sized FP64 device vector from one transport-vector layout to the
+ * other (a tiled device transpose; in and out must not overlap).  Every other
+ * entry point takes RIGHT vectors, so a caller built with the LEFT layout
+ * converts at this boundary (src/tvector.hpp:47-51). */
+int allium_sweep_relayout(allium_sweep* s, const double* in, int in_layout, double* out, int out_layout);
 
 /* DiscreteToMoment::MultTranspose (accumulate = 0) and AddMultTranspose
  * (accumulate = 1, psi += alpha * D^T phi) (src/transport_op.cpp:33-89). */

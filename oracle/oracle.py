@@ -83,6 +83,23 @@ def planck_spectrum(bounds, T, kind=0):
     return out
 
 
+def relayout(psi, G, Nw, ndof, to_left):
+    """Transport-vector layouts of src/tvector.hpp:47-53 (IndexMap<SPACE,
+    ANGLE, ENERGY> for RIGHT, <ENERGY, ANGLE, SPACE> for LEFT): element
+    (g, a, i) sits at i + ndof (a + Nw g) in RIGHT and g + G (a + Nw i) in LEFT,
+    written here as an explicit index scatter."""
+    psi = np.asarray(psi)
+    out = np.empty_like(psi)
+    g, a, i = np.meshgrid(np.arange(G), np.arange(Nw), np.arange(ndof), indexing="ij")
+    right = (i + ndof * (a + Nw * g)).ravel()
+    left = (g + G * (a + Nw * i)).ravel()
+    if to_left:
+        out[left] = psi[right]
+    else:
+        out[right] = psi[left]
+    return out
+
+
 class OracleSweep:
     """InverseAdvectionOperator restated on the CPU (plus D, L, balance, source)."""
 

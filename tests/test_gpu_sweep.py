@@ -41,6 +41,8 @@ CASES = [
     (3, (4, 4, 4), 1, 4, 1, 0.0, 7),
     (3, (4, 3, 3), 2, 4, 1, 0.0, 0),
     (3, (4, 4, 4), 2, 6, 2, 0.1, 0),
+    (3, (3, 3, 2), 3, 4, 1, 0.0, 0),
+    (3, (3, 3, 3), 3, 2, 2, 0.1, 0),
 ]
 
 
@@ -181,7 +183,7 @@ def test_time_absorption(dim, cells):
 
 
 @pytest.mark.parametrize("dim,cells,p", [(1, (10,), 3), (2, (10, 10), 2), (2, (10, 10), 3), (3, (6, 6, 6), 1),
-                                         (3, (10, 10, 10), 0), (3, (3, 3, 3), 2)])
+                                         (3, (10, 10, 10), 0), (3, (3, 3, 3), 2), (3, (3, 3, 3), 3)])
 def test_constant_solution(dim, cells, p):
     # test_sweep.cpp:7-108 on the GPU: sigma = 0, q = 0, unit inflow -> psi == 1
     mesh = M.cartesian(cells)
@@ -369,7 +371,7 @@ def test_errors_are_reported():
     mesh, quad, sig = problem(2, (4, 4), 1)
     m3, q3, s3 = problem(3, (2, 2, 2), 3)
     with pytest.raises(AlliumError) as e:
-        InverseAdvectionOperator(m3, 3, q3, s3)
+        InverseAdvectionOperator(m3, 4, q3, s3)   # p > 3
     assert e.value.status == 7
     L = InverseAdvectionOperator(mesh, 1, quad, sig)
     x = np.zeros(L.width)
@@ -391,6 +393,7 @@ REFL_CASES = [
     (3, (5, 4, 3), 1, 4, 2, (3, 4, 6)),
     (3, (6, 6, 6), 1, 12, 1, (1, 2, 5)),
     (3, (4, 3, 3), 2, 4, 1, (3,)),
+    (3, (3, 3, 2), 3, 4, 1, (2, 5)),
 ]
 
 
@@ -520,3 +523,42 @@ def test_pinned_host_mult_pipeline(dim, cells, sn, G):
     h_io = src.clone().pin_memory()
     L.Mult(h_io, h_io)
     assert torch.equal(h_io, ref.cpu())
+    # the pipeline's shape (slices, compute streams) changes nothing
+    for chunks, streams in [(2, 1), (4, 4), (16, 3), (32, 2)]:
+        L.SetPipeline(chunks, streams)
+        h_psi.zero_()
+        L.Mult(h_src, h_psi)
+        assert torch.equal(h_psi, ref.cpu()), (chunks, streams)
+    with pytest.raises(AlliumError):
+        L.SetPipeline(1, 2)
+    with pytest.raises(AlliumError):
+        L.SetPipeline(8, 5)
+
+
+@pytest.mark.parametrize("dim,cells,p,sn,G", [(2, (9, 7), 1, 4, 3), (3, (4, 3, 3), 2, 4, 2), (1, (33,), 0, 8, 1)])
+def test_left_layout(dim, cells, p, sn, G):
+    # a caller built with the LEFT layout (tvector.hpp:47-53) converts at the
+    # boundary: relayout -> Mult -> relayout equals the oracle's sweep in LEFT
+    from oracle.oracle import relayout
+    mesh, quad, sig, o, L = build(dim, cells, p, sn, G, 0.0, 0)
+    rng = np.random.default_rng(3)
+    src_r = rng.random(o.psi_size)
+    ref_left = relayout(o.mult(src_r), G, quad.size, L.ndof, to_left=True)
+    src_left = torch.from_numpy(relayout(src_r, G, quad.size, L.ndof, to_left=True)).cuda()
+    right = torch.empty_like(src_left)
+    L.Relayout(src_left, L.LEFT, right, L.RIGHT)
+    L.synchronize()
+    assert np.array_equal(right.cpu().numpy(), src_r)   # bit-exact permutation
+    L.Mult(right, right)
+    out_left = torch.empty_like(right)
+    L.Relayout(right, L.RIGHT, out_left, L.LEFT)
+    L.synchronize()
+    assert rel_err(out_left.cpu().numpy(), ref_left) < TOL64
+    same = torch.empty_like(right)
+    L.Relayout(right, L.RIGHT, same, L.RIGHT)
+    L.synchronize()
+    assert torch.equal(same, right)
+    with pytest.raises(AlliumError):
+        L.Relayout(right, L.RIGHT, right, L.LEFT)      # in place is refused
+    with pytest.raises(AlliumError):
+        L.Relayout(right, 2, out_left, L.LEFT)

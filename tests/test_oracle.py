@@ -274,3 +274,17 @@ def test_reflective_errors():
     # adjacent reflective sides (a symmetric quarter) stay a DAG
     o.set_reflective([2, 3])
     assert o.levels()[0] > 0
+
+
+def test_layout_maps():
+    # test_linalg.cpp:116-135: extents (G, Nw, Ndof) = (2, 4, 8); LEFT is Kokkos
+    # layout_left (g fastest), RIGHT layout_right (i fastest)
+    from oracle.oracle import relayout
+    G, Nw, nd = 2, 4, 8
+    right = np.arange(G * Nw * nd, dtype=np.float64)   # value = RIGHT offset
+    left = relayout(right, G, Nw, nd, to_left=True)
+    assert left[1 + 2 * (2 + 4 * 3)] == 3 + 8 * (2 + 4 * 1)   # (g, a, i) = (1, 2, 3)
+    assert left[0 + 2 * (1 + 4 * 6)] == 6 + 8 * (1 + 4 * 0)   # (0, 1, 6)
+    assert np.array_equal(relayout(left, G, Nw, nd, to_left=False), right)
+    # the LEFT vector is the RIGHT one viewed as [G][Nw][Ndof] and transposed
+    assert np.array_equal(left, right.reshape(G, Nw, nd).transpose(2, 1, 0).ravel())
