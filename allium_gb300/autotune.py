@@ -68,15 +68,16 @@ def autotune(L, reps=3, blocks=(32, 64, 128), fp32=True, schedules=None):
     return out
 
 
-def autotune_pipeline(L, h_src, h_psi, reps=3, shapes=((8, 4), (8, 3), (8, 2), (4, 4), (16, 4), (6, 3))):
-    """Pick the (slices, compute streams) of the pinned-host-buffer Mult: each
-    shape is timed on the host clock (the call returns once psi is back in
-    host memory) after two untimed calls, median of `reps`; the fastest is set
-    on the handle.  Returns {"best": {...}, "trials": [...]}."""
+def autotune_pipeline(L, h_src, h_psi, reps=3,
+                      shapes=((8, 4, 1), (8, 4, 0), (8, 4, 2), (8, 3, 1), (10, 4, 2), (6, 4, 1), (12, 4, 2))):
+    """Pick the (slices, compute streams, end taper) of the pinned-host-buffer
+    Mult: each shape is timed on the host clock (the call returns once psi is
+    back in host memory) after two untimed calls, median of `reps`; the
+    fastest is set on the handle.  Returns {"best": {...}, "trials": [...]}."""
     import time
     trials = []
-    for chunks, streams in shapes:
-        L.SetPipeline(chunks, streams)
+    for chunks, streams, taper in shapes:
+        L.SetPipeline(chunks, streams, taper)
         L.Mult(h_src, h_psi)
         L.Mult(h_src, h_psi)
         ts = []
@@ -85,7 +86,7 @@ def autotune_pipeline(L, h_src, h_psi, reps=3, shapes=((8, 4), (8, 3), (8, 2), (
             L.Mult(h_src, h_psi)
             ts.append(time.perf_counter() - t0)
         ts.sort()
-        trials.append({"chunks": chunks, "streams": streams, "ms": 1e3 * ts[len(ts) // 2]})
+        trials.append({"chunks": chunks, "streams": streams, "taper": taper, "ms": 1e3 * ts[len(ts) // 2]})
     best = min(trials, key=lambda t: t["ms"])
-    L.SetPipeline(best["chunks"], best["streams"])
+    L.SetPipeline(best["chunks"], best["streams"], best["taper"])
     return {"best": best, "trials": trials}

@@ -325,7 +325,7 @@ static bool pinned_host(const void* p) {
 static int mult_host_chunked(Handle& h, const double* source, double* psi) {
     const int C = h.pipe_chunks < h.Nw / 2 ? h.pipe_chunks : h.Nw / 2;
     const int S = h.pipe_streams < C ? h.pipe_streams : C;
-    if (int st = allium::build_chunks(h, C)) return st;
+    if (int st = allium::build_chunks(h, C, h.pipe_taper)) return st;
     const auto mk = [](cudaStream_t* st) {
         return *st ? cudaSuccess : cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
     };
@@ -686,12 +686,13 @@ int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads) {
     return ALLIUM_OK;
 }
 
-int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams) {
+int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int taper) {
     if (!s || chunks < 2 || chunks > allium::Handle::kMaxPipeChunks || streams < 1 ||
-        streams > allium::Handle::kMaxPipeStreams)
+        streams > allium::Handle::kMaxPipeStreams || taper < 0 || taper > 3)
         return ALLIUM_ERR_ARG;
     s->h.pipe_chunks = chunks;
     s->h.pipe_streams = streams;
+    s->h.pipe_taper = taper;
     return ALLIUM_OK;
 }
 

@@ -68,7 +68,7 @@ struct Handle {
     uint8_t* d_nbrmap = nullptr;
     FaceOrient* d_orient = nullptr;   // [ne][2 dim]
     // angle chunks of the host-buffer Mult (copy / sweep / copy pipeline):
-    // nodes of chunk c in (level, cell, angle) order, their positions in the
+    // nodes of chunk c in (level, face pattern, cell, angle) order, their positions in the
     // full level order, offsets [nchunk][num_levels + 1]; copy streams,
     // compute streams (comp[0] unused: h.stream) and events.  pipe_chunks
     // and pipe_streams are the requested chunk count and compute streams.
@@ -76,7 +76,9 @@ struct Handle {
     static constexpr int kMaxPipeStreams = 4;
     int pipe_chunks = 8;
     int pipe_streams = 4;
+    int pipe_taper = 1;
     int nchunk = 0;
+    int chunk_taper = 0;
     std::vector<int> h_chunk_angle;   // [nchunk + 1] first angle of each chunk
     int* d_chunk_nodes = nullptr;
     int* d_chunk_pos = nullptr;
@@ -221,7 +223,8 @@ cudaError_t launch_face_dots(Handle& h);
 cudaError_t launch_assemble(Handle& h);
 int compute_reflections(Handle& h, const std::vector<int>& refl_faces);   // allium status
 cudaError_t launch_relayout(Handle& h, const double* in, double* out, int to_left);
-int build_chunks(Handle& h, int nchunk);                                     // allium status
+std::vector<int> chunk_bounds(int Nw, int nchunk, int taper);
+int build_chunks(Handle& h, int nchunk, int taper);                                     // allium status
 cudaError_t launch_sweep_chunk(Handle& h, double* stage, int c, cudaStream_t stream);
 
 // thermal radiative transfer operators (trt.cu)

@@ -429,6 +429,28 @@ __global__ void k_kahn(int Nw, int dim, const double* __restrict__ dots,
     }
 }
 
+// Sort key of node v = (e, a): its level, then the kind of each face (2 bits:
+// none, outflow, inflow from a neighbour, reflective inflow; the branches of
+// the node kernels).  Nodes of one level that share the pattern run in the
+// same warps, so a warp does not issue both sides of a face branch; on the
+// FP64 pipe every issued warp instruction costs its full width.
+__global__ void k_level_keys(long long n, int Nw, int dim, int pattern_bits, const double* __restrict__ dots,
+                             const Slot* __restrict__ slots, const int* __restrict__ level, int* __restrict__ keys) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int e = (int)(v / Nw), a = (int)(v % Nw), nface = 2 * dim;
+    int pat = 0;
+    if (pattern_bits)
+        for (int k = 0; k < nface; ++k) {
+            const Slot s = slots[(size_t)e * nface + k];
+            const double d1 = dots[(size_t)s.face * Nw + a];
+            const double dk = s.side ? -d1 : d1;
+            const int code = dk > 0.0 ? 1 : (dk < 0.0 ? (s.nbr >= 0 ? 2 : (s.nbr <= -2 ? 3 : 0)) : 0);
+            pat |= code << (2 * k);
+        }
+    keys[v] = (level[v] << pattern_bits) | pat;
+}
+
 __global__ void k_iota(int* x, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = (int)i;
@@ -477,18 +499,25 @@ int compute_levels(Handle& h) {
         return ALLIUM_ERR_NOT_DAG;
     }
     h.num_levels = lev;
-    // nodes sorted by level, stable in node id -> (level, cell, angle) order
+    // nodes sorted by (level, face pattern), stable in node id -> within a
+    // level, nodes of one face pattern in (cell, angle) order
+    int* d_key_in = nullptr;
+    CK(cudaMalloc(&d_key_in, N * sizeof(int)));
     CK(cudaMalloc(&d_keys, N * sizeof(int)));
     CK(cudaMalloc(&d_vals, N * sizeof(int)));
+    int level_bits = 1;
+    while ((1 << level_bits) <= lev) ++level_bits;
+    const int pattern_bits = (level_bits + 4 * h.dim <= 31) ? 4 * h.dim : 0;
+    k_level_keys<<<gN, b, 0, h.stream>>>(N, h.Nw, h.dim, pattern_bits, h.d_dots, h.d_slots, h.d_level, d_key_in);
+    CK(cudaGetLastError());
     k_iota<<<gN, b, 0, h.stream>>>(d_vals, N);
     CK(cudaGetLastError());
-    int end_bit = 1;
-    while ((1 << end_bit) <= lev) ++end_bit;
+    const int end_bit = level_bits + pattern_bits;
     size_t tmp_bytes = 0;
-    CK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, h.d_level, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
+    CK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, d_key_in, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
     void* tmp = nullptr;
     CK(cudaMalloc(&tmp, tmp_bytes));
-    CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, h.d_level, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
+    CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, d_key_in, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
     int* d_hist = nullptr;
     CK(cudaMalloc(&d_hist, lev * sizeof(int)));
     CK(cudaMemsetAsync(d_hist, 0, lev * sizeof(int), h.stream));
@@ -499,20 +528,18 @@ int compute_levels(Handle& h) {
     CK(cudaStreamSynchronize(h.stream));
     h.h_level_offsets.assign(lev + 1, 0);
     for (int l = 0; l < lev; ++l) h.h_level_offsets[l + 1] = h.h_level_offsets[l] + hist[l];
-    cudaFree(d_hist); cudaFree(tmp); cudaFree(d_vals); cudaFree(d_keys); cudaFree(d_cnt);
+    cudaFree(d_hist); cudaFree(tmp); cudaFree(d_vals); cudaFree(d_keys); cudaFree(d_key_in); cudaFree(d_cnt);
     return ALLIUM_OK;
 }
 
 // ------------------------------------------------------------ angle chunks
 // key of level-order position t: chunk(angle) * num_levels + level
-__global__ void k_chunk_keys(long long n, int Nw, int nchunk, int nlev, const int* __restrict__ level_nodes,
-                             const int* __restrict__ level, int* __restrict__ keys) {
+__global__ void k_chunk_keys(long long n, int Nw, int nlev, const int* __restrict__ angle_chunk,
+                             const int* __restrict__ level_nodes, const int* __restrict__ level, int* __restrict__ keys) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int node = level_nodes[t];
-    const int a = node % Nw;
-    const int c = (int)(((long long)a * nchunk) / Nw);
-    keys[t] = c * nlev + level[node];
+    keys[t] = angle_chunk[node % Nw] * nlev + level[node];
 }
 
 __global__ void k_gather_nodes(long long n, const int* __restrict__ pos, const int* __restrict__ level_nodes,
@@ -521,11 +548,33 @@ __global__ void k_gather_nodes(long long n, const int* __restrict__ pos, const i
     if (u < n) out[u] = level_nodes[pos[u]];
 }
 
+// First angle of each of the nchunk contiguous blocks of angles.  Chunk
+// weights 1 except the first and the last, which get 1/2^taper: small end
+// chunks shorten the pipeline's fill (the first copy in) and drain (the last
+// sweep and copy out).  Every chunk keeps at least one angle.
+std::vector<int> chunk_bounds(int Nw, int nchunk, int taper) {
+    std::vector<double> w(nchunk, 1.0);
+    if (nchunk >= 3) w[0] = w[nchunk - 1] = 1.0 / (1 << taper);
+    double W = 0.0;
+    for (double x : w) W += x;
+    std::vector<int> b(nchunk + 1, 0);
+    double run = 0.0;
+    for (int c = 1; c < nchunk; ++c) {
+        run += w[c - 1];
+        int v = (int)std::lround(Nw * run / W);
+        if (v < b[c - 1] + 1) v = b[c - 1] + 1;
+        if (v > Nw - (nchunk - c)) v = Nw - (nchunk - c);
+        b[c] = v;
+    }
+    b[nchunk] = Nw;
+    return b;
+}
+
 // Orders for the chunked host-buffer Mult: angles split into nchunk contiguous
-// blocks (angle a in chunk a * nchunk / Nw); within a chunk the nodes keep the
-// (level, cell, angle) order of the full sweep (stable sort on the key).
-int build_chunks(Handle& h, int nchunk) {
-    if (h.nchunk == nchunk) return ALLIUM_OK;
+// blocks (chunk_bounds); within a chunk the nodes keep the order of the full
+// sweep (stable sort on the key).
+int build_chunks(Handle& h, int nchunk, int taper) {
+    if (h.nchunk == nchunk && h.chunk_taper == taper) return ALLIUM_OK;
     // the captured chunk sweeps (graph kinds 40 + c) hold the old chunk offsets
     CK(cudaStreamSynchronize(h.stream));
     drop_graphs(h);
@@ -543,7 +592,14 @@ int build_chunks(Handle& h, int nchunk) {
     CK(cudaMalloc(&d_vals, N * sizeof(int)));
     CK(cudaMalloc(&h.d_chunk_pos, N * sizeof(int)));
     CK(cudaMalloc(&h.d_chunk_nodes, N * sizeof(int)));
-    k_chunk_keys<<<gN, b, 0, h.stream>>>(N, h.Nw, nchunk, L, h.d_level_nodes, h.d_level, d_keys);
+    const std::vector<int> bounds = chunk_bounds(h.Nw, nchunk, taper);
+    std::vector<int> angle_chunk(h.Nw);
+    for (int c = 0; c < nchunk; ++c)
+        for (int a = bounds[c]; a < bounds[c + 1]; ++a) angle_chunk[a] = c;
+    int* d_angle_chunk = nullptr;
+    CK(cudaMalloc(&d_angle_chunk, (size_t)h.Nw * sizeof(int)));
+    CK(cudaMemcpyAsync(d_angle_chunk, angle_chunk.data(), (size_t)h.Nw * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    k_chunk_keys<<<gN, b, 0, h.stream>>>(N, h.Nw, L, d_angle_chunk, h.d_level_nodes, h.d_level, d_keys);
     CK(cudaGetLastError());
     k_iota<<<gN, b, 0, h.stream>>>(d_vals, N);
     CK(cudaGetLastError());
@@ -572,10 +628,10 @@ int build_chunks(Handle& h, int nchunk) {
         for (int l = 0; l < L; ++l) { o[l] = run; run += hist[(size_t)c * L + l]; }
         o[L] = run;
     }
-    h.h_chunk_angle.assign(nchunk + 1, 0);
-    for (int c = 0; c <= nchunk; ++c) h.h_chunk_angle[c] = (int)(((long long)c * h.Nw + nchunk - 1) / nchunk);
-    cudaFree(d_hist); cudaFree(tmp); cudaFree(d_vals); cudaFree(d_keys2); cudaFree(d_keys);
+    h.h_chunk_angle = bounds;
+    cudaFree(d_hist); cudaFree(tmp); cudaFree(d_vals); cudaFree(d_keys2); cudaFree(d_keys); cudaFree(d_angle_chunk);
     h.nchunk = nchunk;
+    h.chunk_taper = taper;
     return ALLIUM_OK;
 }
 

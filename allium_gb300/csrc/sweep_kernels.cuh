@@ -83,6 +83,28 @@ __device__ __forceinline__ int apply_fixup(int kind, R xmin, const R (&w)[N], R 
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Sign tests and sign flips of Omega.n on the bit pattern, on the integer
+// pipe: GB300 issues every FP64 compare or negate on its narrow FP64 pipe,
+// which the node kernels already fill with FMAs.  below_zero(x) == (x < 0)
+// and above_zero(x) == (x > 0) for every non-NaN x (-0.0 is neither);
+// negate_if(x, f) == (f ? -x : x) bit for bit.
+__device__ __forceinline__ bool below_zero(double x) {
+    const long long b = __double_as_longlong(x);
+    return b < 0 && (b << 1) != 0;
+}
+__device__ __forceinline__ bool below_zero(float x) {
+    const int b = __float_as_int(x);
+    return b < 0 && (b << 1) != 0;
+}
+__device__ __forceinline__ bool above_zero(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool above_zero(float x) { return __float_as_int(x) > 0; }
+__device__ __forceinline__ double negate_if(double x, bool f) {
+    return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(x) ^ ((unsigned long long)f << 63)));
+}
+__device__ __forceinline__ float negate_if(float x, bool f) {
+    return __int_as_float((int)((unsigned)__float_as_int(x) ^ ((unsigned)f << 31)));
+}
+
 // n contiguous values of one (group, angle, cell) block; 16-byte vectors when
 // the block size allows (the API requires 16-byte aligned vectors)
 template <int N, typename R>
@@ -290,10 +312,10 @@ __device__ __forceinline__ void assemble_local(const SweepArgs<R>& s, int e, int
     for (int k = 0; k < NFACE; ++k) {
         const Slot q = s.slots[(size_t)e * NFACE + k];
         const R d1 = s.dots[(size_t)q.face * s.Nw + a];
-        const R dk = q.side ? -d1 : d1;
+        const R dk = negate_if(d1, q.side);
         dots[k] = dk;
         nbrs[k] = q.nbr;
-        if (dk > R(0)) {
+        if (above_zero(dk)) {
             const R* F = s.F + ((size_t)e * NFACE + k) * NF * NF;
 #pragma unroll
             for (int ii = 0; ii < NF; ++ii) {
@@ -324,7 +346,7 @@ __device__ __forceinline__ void assemble_rhs(const SweepArgs<R>& s, int e, int a
     load_block<N>(s.src + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), b);
 #pragma unroll
     for (int k = 0; k < NFACE; ++k) {
-        if (dots[k] < R(0) && nbrs[k] >= 0) {
+        if (below_zero(dots[k]) && nbrs[k] >= 0) {
             const uint8_t* map = s.nbrmap + ((size_t)e * NFACE + k) * NF;
             const R* up = s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)nbrs[k] * N);
             R u[NF];
@@ -349,7 +371,7 @@ __device__ __forceinline__ void assemble_rhs(const SweepArgs<R>& s, int e, int a
                 const int fi = face_dof(D, P, k, ii);
                 b[fi] = fma_r(rd, acc, b[fi]);
             }
-        } else if (dots[k] < R(0) && nbrs[k] <= -2) {
+        } else if (below_zero(dots[k]) && nbrs[k] <= -2) {
             // reflective face: the same cell's trace in the reflected direction
             // (sweep.cpp:432-437), face block F(self, self)
             const int ar = s.refl[(size_t)(-2 - nbrs[k]) * s.Nw + a];
@@ -759,7 +781,7 @@ __global__ void __launch_bounds__(128) k_sweep_cached_level(SweepArgs<R> s, cons
     for (int k = 0; k < NFACE; ++k) {
         const Slot q = s.slots[(size_t)e * NFACE + k];
         const R d1 = s.dots[(size_t)q.face * s.Nw + a];
-        dots[k] = q.side ? -d1 : d1;
+        dots[k] = negate_if(d1, q.side);
         nbrs[k] = q.nbr;
     }
     R b[N];
@@ -1050,7 +1072,7 @@ __device__ __forceinline__ void wait_upwind(const FlowArgs& f, int Nw, int G, in
                                             const int (&nbrs)[2 * D], unsigned epoch, int* status) {
 #pragma unroll
     for (int k = 0; k < 2 * D; ++k)
-        if (dots[k] < R(0) && nbrs[k] >= 0)
+        if (below_zero(dots[k]) && nbrs[k] >= 0)
             wait_flag(f.flags + ((size_t)nbrs[k] * Nw + a) * G + g, epoch, status);
 }
 
@@ -1065,7 +1087,7 @@ __device__ __forceinline__ void face_info(const SweepArgs<R>& s, int e, int a, R
     for (int k = 0; k < 2 * D; ++k) {
         const Slot q = s.slots[(size_t)e * 2 * D + k];
         const R d1 = s.dots[(size_t)q.face * s.Nw + a];
-        dots[k] = q.side ? -d1 : d1;
+        dots[k] = negate_if(d1, q.side);
         nbrs[k] = q.nbr;
     }
 }

@@ -78,7 +78,7 @@ cudaError_t sweep_levels_cached(Handle& h, const SweepArgs<R>& args, const R* in
     return cudaGetLastError();
 }
 
-// One angle chunk of the sweep: the chunk's nodes in (level, cell, angle)
+// One angle chunk of the sweep: the chunk's nodes in (level, face pattern, cell, angle)
 // order (h.d_chunk_nodes), its own level ranges; the stored inverses found
 // through each node's position in the full level order.
 template <int D, int P>

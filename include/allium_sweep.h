@@ -169,10 +169,12 @@ int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads);
  * stored inverses, inflow boundaries): the directions are cut into `chunks`
  * contiguous slices (2..32, at most half the directions), each copied in,
  * swept and copied out on its own, and the sweeps of consecutive slices
- * alternate over `streams` compute streams (1..4).  Default 8 and 4.  No
- * reference counterpart (the reference's vectors are host memory).  Results
- * do not depend on either knob. */
-int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams);
+ * alternate over `streams` compute streams (1..4).  With taper t (0..3) the
+ * first and last slices get 1/2^t of the others' share of directions, which
+ * shortens the pipeline's fill and drain.  Default 8, 4, 1.  No reference
+ * counterpart (the reference's vectors are host memory).  Results do not
+ * depend on the shape. */
+int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int taper);
 
 /* Negative-flux fixup inside the sweep (SetFixupOperator / UseFixup,
  * src/sweep.hpp:108-117, applied at src/sweep.cpp:465-470): kind 0 off,

@@ -524,15 +524,17 @@ def test_pinned_host_mult_pipeline(dim, cells, sn, G):
     L.Mult(h_io, h_io)
     assert torch.equal(h_io, ref.cpu())
     # the pipeline's shape (slices, compute streams) changes nothing
-    for chunks, streams in [(2, 1), (4, 4), (16, 3), (32, 2)]:
-        L.SetPipeline(chunks, streams)
+    for chunks, streams, taper in [(2, 1, 0), (4, 4, 1), (16, 3, 2), (32, 2, 3), (8, 4, 3)]:
+        L.SetPipeline(chunks, streams, taper)
         h_psi.zero_()
         L.Mult(h_src, h_psi)
-        assert torch.equal(h_psi, ref.cpu()), (chunks, streams)
+        assert torch.equal(h_psi, ref.cpu()), (chunks, streams, taper)
     with pytest.raises(AlliumError):
         L.SetPipeline(1, 2)
     with pytest.raises(AlliumError):
         L.SetPipeline(8, 5)
+    with pytest.raises(AlliumError):
+        L.SetPipeline(8, 4, 4)
 
 
 @pytest.mark.parametrize("dim,cells,p,sn,G", [(2, (9, 7), 1, 4, 3), (3, (4, 3, 3), 2, 4, 2), (1, (33,), 0, 8, 1)])
