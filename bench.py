@@ -361,6 +361,38 @@ def batch_section(count):
     return out
 
 
+def warm_solver_libraries():
+    """Untimed: one pass of every solver path on a 6x6 problem and a few
+    training steps of the cell network.  On a fresh
+    machine the first call into cuSOLVER (GMRES's least squares), cuSPARSE and
+    a few torch kernels loads and initialises those libraries, seconds per
+    library; none of that belongs in a solver's time."""
+    import torch
+    from allium_gb300 import mesh as M
+    from allium_gb300 import quadrature as Q
+    from allium_gb300.dsa import DSAPreconditioner
+    from allium_gb300.solvers import SchurOperator, refine, solve_gmres, source_iteration
+    from allium_gb300.sweep import FormTransportSource, InverseAdvectionOperator
+    mesh = M.cartesian((6, 6))
+    ne = mesh.num_elements
+    sig_t, sig_s, q = np.ones((1, ne)), np.full((1, ne), 0.9), np.ones((1, ne))
+    L = InverseAdvectionOperator(mesh, 1, Q.level_symmetric(4, 2), sig_t)
+    src = torch.from_numpy(FormTransportSource(L, q)).cuda()
+    for vcycle in (False, True):
+        dsa = DSAPreconditioner(L, sig_s, cg_tol=1e-6, cg_maxiter=20, vcycle=vcycle)
+        source_iteration(SchurOperator(L, sig_s), src, tol=1e-6, dsa=dsa)
+        solve_gmres(SchurOperator(L, sig_s), src, tol=1e-6, restart=30, maxiter=40, prec=dsa)
+        refine(SchurOperator(L, sig_s), src, tol=1e-6, inner_tol=1e-3, restart=30, prec=dsa)
+    from allium_gb300.mlp import CellMLP
+    net = CellMLP(8, 4, width=256, layers=4, seed=0)
+    X = torch.randn(4096, 8, device="cuda")
+    Y = torch.randn(4096, 4, device="cuda")
+    for _ in range(3):
+        net.train_step(X[torch.randperm(4096, device="cuda")].contiguous(), (Y - Y.mean(0)) / Y.std(0))
+    net.forward(X)
+    torch.cuda.synchronize()
+
+
 def chive2d_section(cpu=True):
     """The 2D chive configuration: 64x64 quads, p = 1, S8, sigma_t = 1,
     sigma_s = 0.9, q = 1, vacuum; source iteration to 1e-8 relative change of
@@ -598,6 +630,7 @@ def run_gpu(args):
                            "note": "node-major layout (the refinement's inner sweep), from an FP32 copy of the stored inverses"},
             "clocks": clk.summary()}
     if not args.no_solve:
+        warm_solver_libraries()
         line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0])
         line["chive_2d"] = chive2d_section(cpu=not args.no_cpu)
         line["trt_marshak"] = trt_section(args.trt_steps)
