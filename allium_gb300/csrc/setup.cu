@@ -461,6 +461,39 @@ __global__ void k_level_hist(const int* __restrict__ level, long long n, int* __
     if (i < n) atomicAdd(&hist[level[i]], 1);
 }
 
+// The same histogram with per-block counts in shared memory (nbins ints) and
+// one global add per bin and block: a few hundred bins hit by 10^7..10^8
+// global atomics serialise on the bins.
+__global__ void k_level_hist_shared(const int* __restrict__ level, long long n, int nbins, int* __restrict__ hist) {
+    extern __shared__ int counts[];
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x) counts[k] = 0;
+    __syncthreads();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&counts[level[i]], 1);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x)
+        if (counts[k]) atomicAdd(&hist[k], counts[k]);
+}
+
+// histogram of n values in [0, nbins) into hist (zeroed here)
+static cudaError_t level_histogram(Handle& h, const int* values, long long n, int nbins, int* hist) {
+    cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)nbins * sizeof(int), h.stream);
+    if (e != cudaSuccess) return e;
+    const int b = 256;
+    if (nbins <= 12288) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        long long grid = (long long)(sms > 0 ? sms : 1) * 8;
+        const long long need = (n + b - 1) / b;
+        if (grid > need) grid = need > 0 ? need : 1;
+        k_level_hist_shared<<<(unsigned)grid, b, (size_t)nbins * sizeof(int), h.stream>>>(values, n, nbins, hist);
+    } else {
+        k_level_hist<<<(unsigned)((n + b - 1) / b), b, 0, h.stream>>>(values, n, hist);
+    }
+    return cudaGetLastError();
+}
+
 #define CK(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { h.last_error = cudaGetErrorString(_e); return ALLIUM_ERR_CUDA; } } while (0)
 
 int compute_levels(Handle& h) {
@@ -520,9 +553,7 @@ int compute_levels(Handle& h) {
     CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, d_key_in, d_keys, d_vals, h.d_level_nodes, (int)N, 0, end_bit, h.stream));
     int* d_hist = nullptr;
     CK(cudaMalloc(&d_hist, lev * sizeof(int)));
-    CK(cudaMemsetAsync(d_hist, 0, lev * sizeof(int), h.stream));
-    k_level_hist<<<gN, b, 0, h.stream>>>(h.d_level, N, d_hist);
-    CK(cudaGetLastError());
+    CK(level_histogram(h, h.d_level, N, lev, d_hist));
     std::vector<int> hist(lev);
     CK(cudaMemcpyAsync(hist.data(), d_hist, lev * sizeof(int), cudaMemcpyDeviceToHost, h.stream));
     CK(cudaStreamSynchronize(h.stream));
@@ -615,9 +646,7 @@ int build_chunks(Handle& h, int nchunk, int taper) {
     CK(cudaGetLastError());
     const int nkeys = nchunk * L;
     CK(cudaMalloc(&d_hist, (size_t)nkeys * sizeof(int)));
-    CK(cudaMemsetAsync(d_hist, 0, (size_t)nkeys * sizeof(int), h.stream));
-    k_level_hist<<<gN, b, 0, h.stream>>>(d_keys, N, d_hist);
-    CK(cudaGetLastError());
+    CK(level_histogram(h, d_keys, N, nkeys, d_hist));
     std::vector<int> hist(nkeys);
     CK(cudaMemcpyAsync(hist.data(), d_hist, (size_t)nkeys * sizeof(int), cudaMemcpyDeviceToHost, h.stream));
     CK(cudaStreamSynchronize(h.stream));
@@ -646,16 +675,18 @@ __global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw
                                                      const double* __restrict__ corners, const double* __restrict__ omega,
                                                      const Slot* __restrict__ slots, const double* __restrict__ qcell,
                                                      const double* __restrict__ inflow, int nattr, double* __restrict__ out) {
+    // one thread per (g, e): the domain term does not depend on the angle, so
+    // it is integrated once and each angle adds its own boundary terms to a
+    // copy (the same sums in the same order as integrating per angle)
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= (long long)G * Nw * ne) return;
+    if (tid >= (long long)G * ne) return;
     const int e = (int)(tid % ne);
-    const long long r = tid / ne;
-    const int a = (int)(r % Nw), g = (int)(r / Nw);
+    const int g = (int)(tid / ne);
     const int dim = t.dim, n = t.n, n1 = t.n1, nc = 1 << dim;
     double X[24];
     for (int q = 0; q < nc * dim; ++q) X[q] = corners[(size_t)e * nc * dim + q];
-    double acc[64];
-    for (int i = 0; i < n; ++i) acc[i] = 0.0;
+    double vol[64];
+    for (int i = 0; i < n; ++i) vol[i] = 0.0;
     const double Q = qcell ? qcell[(size_t)g * ne + e] : 0.0;
     const int m4 = t.rn[4];
     int np = 1;
@@ -674,16 +705,30 @@ __global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw
                 int ii[3]; dof_index(dim, n1, i, ii);
                 double ph = 1.0;
                 for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
-                acc[i] += w * val * ph;
+                vol[i] += w * val * ph;
             }
         }
     }
-    if (inflow) {
+    // boundary faces of this cell that carry a non-zero inflow
+    bool any_inflow = false;
+    if (inflow)
+        for (int k = 0; k < 2 * dim; ++k) {
+            const Slot s = slots[(size_t)e * 2 * dim + k];
+            if (s.nbr < 0 && s.attr >= 0 && s.attr < nattr && inflow[(size_t)g * nattr + s.attr] != 0.0) any_inflow = true;
+        }
+    const int m5 = t.rn[5];
+    int npf = 1;
+    for (int d = 0; d < dim - 1; ++d) npf *= m5;
+    for (int a = 0; a < Nw; ++a) {
+        double* o = out + psi_index(ndof, Nw, g, a, (long long)e * n);
+        if (!any_inflow) {
+            for (int i = 0; i < n; ++i) o[i] = vol[i];
+            continue;
+        }
+        double acc[64];
+        for (int i = 0; i < n; ++i) acc[i] = vol[i];
         double om[3] = {0, 0, 0};
         for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
-        const int m5 = t.rn[5];
-        int npf = 1;
-        for (int d = 0; d < dim - 1; ++d) npf *= m5;
         for (int k = 0; k < 2 * dim; ++k) {
             const Slot s = slots[(size_t)e * 2 * dim + k];
             if (s.nbr >= 0 || s.attr < 0 || s.attr >= nattr) continue;
@@ -711,13 +756,12 @@ __global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw
                 }
             }
         }
+        for (int i = 0; i < n; ++i) o[i] = acc[i];
     }
-    double* o = out + psi_index(ndof, Nw, g, a, (long long)e * n);
-    for (int i = 0; i < n; ++i) o[i] = acc[i];
 }
 
 cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out) {
-    const long long total = (long long)h.G * h.Nw * h.ne;
+    const long long total = (long long)h.G * h.ne;
     const int b = 128;
     k_form_source<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.ref, h.ne, h.Nw, h.G, h.ndof, h.d_corners, h.d_omega,
                                                                        h.d_slots, q_cell, inflow, nattr, out);
