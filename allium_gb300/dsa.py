@@ -4,8 +4,8 @@ MIPDiffusion wraps the C ABI's MIP operator K (InteriorPenaltyDiscretization,
 src/moment_discretization.cpp:73-110) and solves K x = b by preconditioned
 conjugate gradients: allium applies CG with hypre's BoomerAMG; here the
 preconditioner is AggregationVCycle (block-Jacobi smoothing on the DG level,
-the cellwise-constant Galerkin operator and pairwise aggregates below it) or
-plain block-Jacobi (the inverted cell blocks K_ee).  DSAPreconditioner is DiffusionSyntheticAccelerationOperator
+the continuous vertex space and smoothed aggregation below it, all built and
+applied on the device) or plain block-Jacobi (the inverted cell blocks K_ee).  DSAPreconditioner is DiffusionSyntheticAccelerationOperator
 (src/transport_op.hpp:38-59): y = x + K^{-1} (M_s x), M_s the within-group
 scattering mass, for source iteration and as the right preconditioner of GMRES
 on T phi = phi - D L^{-1} D^T M_s phi.
@@ -129,26 +129,105 @@ def _csr_spmv(rowptr, col, val, x, y, alpha=1.0, beta=0.0):
     return y
 
 
+class SparseCOO:
+    """Sparse matrix as (row, col, val) tensors sorted by (row, col), no
+    duplicates, on any torch device; products and sums by expand-sort-reduce."""
+
+    def __init__(self, row, col, val, shape):
+        self.row, self.col, self.val, self.shape = row, col, val, (int(shape[0]), int(shape[1]))
+
+    @staticmethod
+    def coalesce(row, col, val, shape):
+        """Sum the entries that share (row, col)."""
+        ncols = int(shape[1])
+        keys = row.to(torch.int64) * ncols + col.to(torch.int64)
+        uk, inv = torch.unique(keys, return_inverse=True)
+        acc = torch.zeros(uk.numel(), dtype=val.dtype, device=val.device).index_add_(0, inv, val)
+        return SparseCOO(uk // ncols, uk % ncols, acc, shape)
+
+    def rowptr(self):
+        counts = torch.bincount(self.row, minlength=self.shape[0])
+        return torch.cat([torch.zeros(1, dtype=torch.int64, device=counts.device), torch.cumsum(counts, 0)])
+
+    def transpose(self):
+        return SparseCOO.coalesce(self.col, self.row, self.val, (self.shape[1], self.shape[0]))
+
+    def diagonal(self):
+        on = self.row == self.col
+        return torch.zeros(self.shape[0], dtype=self.val.dtype, device=self.val.device).index_add_(
+            0, self.row[on], self.val[on])
+
+    def matmul(self, B):
+        """self @ B: every product a_ik b_kj, then summed per (i, j)."""
+        bptr = B.rowptr()
+        start = bptr[self.col]
+        cnt = bptr[self.col + 1] - start
+        which = torch.repeat_interleave(torch.arange(self.col.numel(), device=cnt.device), cnt)
+        first = torch.cumsum(cnt, 0) - cnt
+        bidx = start[which] + (torch.arange(which.numel(), device=cnt.device) - first[which])
+        return SparseCOO.coalesce(self.row[which], B.col[bidx], self.val[which] * B.val[bidx],
+                                  (self.shape[0], B.shape[1]))
+
+    def spmv_csr(self, dev):
+        """(rowptr, col, val, nrows) with int32 indices for allium_csr_spmv."""
+        return (self.rowptr().to(torch.int32).to(dev), self.col.to(torch.int32).to(dev),
+                self.val.to(torch.float64).to(dev), self.shape[0])
+
+    def to_dense(self):
+        out = torch.zeros(self.shape, dtype=self.val.dtype, device=self.val.device)
+        out[self.row, self.col] = self.val
+        return out
+
+
+def _pairs(A):
+    """One round of greedy pairwise matching (allium_pair_aggregates) on a host
+    copy of A; returns (aggregate of every row, count)."""
+    rp = np.ascontiguousarray(A.rowptr().cpu().numpy(), dtype=np.int32)
+    cl = np.ascontiguousarray(A.col.cpu().numpy(), dtype=np.int32)
+    vl = np.ascontiguousarray(A.val.cpu().numpy(), dtype=np.float64)
+    agg = np.empty(A.shape[0], dtype=np.int32)
+    nagg = _lib.lib().allium_pair_aggregates(A.shape[0], rp.ctypes.data, cl.ctypes.data, vl.ctypes.data,
+                                             agg.ctypes.data)
+    return torch.from_numpy(agg.astype(np.int64)).to(A.row.device), nagg
+
+
 def _pair_aggregates(A):
-    """Two rounds of greedy pairwise aggregation (allium_pair_aggregates):
-    aggregates of up to four rows; returns (aggregate of every row, count)."""
-    import scipy.sparse as sp
-    L = _lib.lib()
-
-    def once(M):
-        M = M.tocsr()
-        M.sort_indices()
-        rp = np.ascontiguousarray(M.indptr, dtype=np.int32)
-        cl = np.ascontiguousarray(M.indices, dtype=np.int32)
-        vl = np.ascontiguousarray(M.data, dtype=np.float64)
-        agg = np.empty(M.shape[0], dtype=np.int32)
-        nagg = L.allium_pair_aggregates(M.shape[0], rp.ctypes.data, cl.ctypes.data, vl.ctypes.data, agg.ctypes.data)
-        return agg.astype(np.int64), nagg
-
-    a1, n1 = once(A)
-    P1 = sp.csr_matrix((np.ones(A.shape[0]), (np.arange(A.shape[0]), a1)), shape=(A.shape[0], n1))
-    a2, n2 = once(P1.T @ A @ P1)
+    """Two rounds of greedy pairwise aggregation: aggregates of up to four
+    rows; returns (aggregate of every row, count)."""
+    a1, n1 = _pairs(A)
+    A1 = SparseCOO.coalesce(a1[A.row], a1[A.col], A.val, (n1, n1))   # T1^T A T1
+    a2, n2 = _pairs(A1)
     return a2[a1], n2
+
+
+def smoothed_aggregation_levels(A, coarse=400):
+    """Levels of the smoothed-aggregation hierarchy below the vertex operator
+    A (a SparseCOO): per level the operator, its inverse diagonal and, except
+    for the last, the prolongator P = (I - 4/(3 lam) D^-1 A) T (T the
+    aggregate indicator, lam the largest absolute row sum of D^-1 A) and
+    R = P^T; the next operator is R A P.  The last level keeps the operator
+    for a dense solve."""
+    levels = []
+    while True:
+        d = A.diagonal()
+        lvl = {"A": A, "dinv": 1.0 / d}
+        levels.append(lvl)
+        if A.shape[0] <= coarse:
+            break
+        agg, nagg = _pair_aggregates(A)
+        n = A.shape[0]
+        rowsum = torch.zeros(n, dtype=A.val.dtype, device=A.val.device).index_add_(0, A.row, A.val.abs())
+        lam = float((rowsum / d.abs()).max())
+        AT = SparseCOO.coalesce(A.row, agg[A.col], A.val, (n, nagg))
+        w = 4.0 / 3.0 / lam
+        ar = torch.arange(n, device=A.row.device)
+        P = SparseCOO.coalesce(torch.cat([ar, AT.row]), torch.cat([agg, AT.col]),
+                               torch.cat([torch.ones(n, dtype=A.val.dtype, device=A.val.device),
+                                          -w * AT.val / d[AT.row]]), (n, nagg))
+        R = P.transpose()
+        lvl["P"], lvl["R"] = P, R
+        A = R.matmul(A.matmul(P))
+    return levels
 
 
 def _gll_nodes(p):
@@ -183,28 +262,22 @@ def _corner_weights(dim, order):
 _CORNER_TO_MFEM = {1: [0, 1], 2: [0, 1, 3, 2], 3: [0, 1, 3, 2, 4, 5, 7, 6]}
 
 
-def _vertex_prolongation(mesh, order, G):
-    """P: continuous multilinear vertex values -> DG nodal values, for G
-    independent groups (rows g * Ndof + e * n + i, columns g * Nv + v)."""
-    import scipy.sparse as sp
+def _vertex_prolongation(mesh, order, G, dev):
+    """P (a SparseCOO on dev): continuous multilinear vertex values -> DG nodal
+    values, for G independent groups (rows g * Ndof + e * n + i, columns
+    g * Nv + v)."""
     dim = mesh.dim
-    W = _corner_weights(dim, order)
-    n = W.shape[0]
+    W = torch.from_numpy(_corner_weights(dim, order)).to(dev)      # [n][corners]
+    n, nc = W.shape
     ne, nv = mesh.num_elements, mesh.num_vertices
-    verts = mesh.elements[:, _CORNER_TO_MFEM[dim]]                 # [Ne][corners]
-    rows = (np.arange(ne)[:, None, None] * n + np.arange(n)[None, :, None]).repeat(1 << dim, axis=2)
-    cols = np.broadcast_to(verts[:, None, :], rows.shape)
-    vals = np.broadcast_to(W[None, :, :], rows.shape)
+    verts = torch.from_numpy(mesh.elements[:, _CORNER_TO_MFEM[dim]].astype(np.int64)).to(dev)
+    rows = (torch.arange(ne, device=dev)[:, None, None] * n + torch.arange(n, device=dev)[None, :, None]).expand(ne, n, nc)
+    cols = verts[:, None, :].expand(ne, n, nc)
+    vals = W[None, :, :].expand(ne, n, nc)
     keep = vals != 0.0
-    P1 = sp.csr_matrix((vals[keep], (rows[keep], cols[keep])), shape=(ne * n, nv))
-    return sp.block_diag([P1] * G, format="csr")
-
-
-def _device_csr(M, dev):
-    M = M.tocsr()
-    M.sort_indices()
-    return (torch.from_numpy(M.indptr.astype(np.int32)).to(dev), torch.from_numpy(M.indices.astype(np.int32)).to(dev),
-            torch.from_numpy(M.data.astype(np.float64)).to(dev), M.shape[0])
+    r, c, v = rows[keep], cols[keep], vals[keep]
+    return SparseCOO.coalesce(torch.cat([r + g * ne * n for g in range(G)]), torch.cat([c + g * nv for g in range(G)]),
+                              v.repeat(G), (G * ne * n, G * nv))
 
 
 class AggregationVCycle:
@@ -214,10 +287,10 @@ class AggregationVCycle:
     vertex values at the DG nodes; below that smoothed aggregation (aggregates
     of up to four strongly coupled vertices, Jacobi-smoothed tentative
     prolongator, damped Jacobi smoothing) down to a dense solve.  Built on the
-    host from K's blocks once per operator, applied on the device."""
+    device from K's blocks once per operator (the greedy pairing runs on a
+    host copy of each level), applied on the device."""
 
     def __init__(self, mip, omega0=0.7, omega=0.67, coarse=400):
-        import scipy.sparse as sp
         self.mip, self.omega0, self.omega = mip, omega0, omega
         L = mip.L
         G, ne, n, nd = mip.G, L.mesh.num_elements, mip.n, 2 * L.dim
@@ -246,28 +319,17 @@ class AggregationVCycle:
             cols_l.append(cv[m] + g * nv)
             vals_l.append(Cb[g][m])
         del Cb
-        keys = torch.cat(rows_l) * (G * nv) + torch.cat(cols_l)
-        vals = torch.cat(vals_l)
-        uk, inv = torch.unique(keys, return_inverse=True)
-        acc = torch.zeros(uk.numel(), dtype=torch.float64, device=dev).index_add_(0, inv, vals)
-        uk = uk.cpu().numpy()
-        A = sp.csr_matrix((acc.cpu().numpy(), (uk // (G * nv), uk % (G * nv))), shape=(G * nv, G * nv))
-        Pv = _vertex_prolongation(L.mesh, L.order, G)
-        self.P0, self.R0 = _device_csr(Pv, dev), _device_csr(Pv.T, dev)
+        A = SparseCOO.coalesce(torch.cat(rows_l), torch.cat(cols_l), torch.cat(vals_l), (G * nv, G * nv))
+        Pv = _vertex_prolongation(L.mesh, L.order, G, dev)
+        self.P0, self.R0 = Pv.spmv_csr(dev), Pv.transpose().spmv_csr(dev)
         self.levels = []
-        while True:
-            lvl = {"A": _device_csr(A, dev), "dinv": torch.from_numpy(1.0 / A.diagonal()).to(dev), "n": A.shape[0]}
+        for lv in smoothed_aggregation_levels(A, coarse):
+            lvl = {"A": lv["A"].spmv_csr(dev), "dinv": lv["dinv"], "n": lv["A"].shape[0]}
+            if "P" in lv:
+                lvl["P"], lvl["R"] = lv["P"].spmv_csr(dev), lv["R"].spmv_csr(dev)
+            else:
+                lvl["inv"] = torch.from_numpy(np.linalg.inv(lv["A"].to_dense().cpu().numpy())).to(dev)
             self.levels.append(lvl)
-            if A.shape[0] <= coarse:
-                lvl["inv"] = torch.from_numpy(np.linalg.inv(A.toarray())).to(dev)
-                break
-            agg, nagg = _pair_aggregates(A)
-            T = sp.csr_matrix((np.ones(A.shape[0]), (np.arange(A.shape[0]), agg)), shape=(A.shape[0], nagg))
-            Dinv = sp.diags(1.0 / A.diagonal())
-            lam = float(np.max(np.asarray(abs(Dinv @ A).sum(axis=1)).ravel()))
-            P = (T - (4.0 / 3.0 / lam) * (Dinv @ (A @ T))).tocsr()
-            lvl["P"], lvl["R"] = _device_csr(P, dev), _device_csr(P.T, dev)
-            A = (P.T @ A @ P).tocsr()
 
     @staticmethod
     def _mv(M, x, out=None, alpha=1.0, beta=0.0):

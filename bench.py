@@ -362,7 +362,7 @@ def batch_section(count):
 
 
 def warm_solver_libraries():
-    """Untimed: one pass of every solver path on a 6x6 problem and a few
+    """Untimed: one pass of every solver path on a 24x24 problem and a few
     training steps of the cell network.  On a fresh
     machine the first call into cuSOLVER (GMRES's least squares), cuSPARSE and
     a few torch kernels loads and initialises those libraries, seconds per
@@ -373,7 +373,7 @@ def warm_solver_libraries():
     from allium_gb300.dsa import DSAPreconditioner
     from allium_gb300.solvers import SchurOperator, refine, solve_gmres, source_iteration
     from allium_gb300.sweep import FormTransportSource, InverseAdvectionOperator
-    mesh = M.cartesian((6, 6))
+    mesh = M.cartesian((24, 24))   # 625 vertices: one aggregation level below the vertex space
     ne = mesh.num_elements
     sig_t, sig_s, q = np.ones((1, ne)), np.full((1, ne), 0.9), np.ones((1, ne))
     L = InverseAdvectionOperator(mesh, 1, Q.level_symmetric(4, 2), sig_t)
