@@ -165,10 +165,11 @@ class LinearizedTRT:
     mesh/order/quad: the sweep's discretisation; bounds[G+1], nu[G]: group
     bounds and midpoints; opacity (C, a, b): sigma_g = C nu_g^a T^b; cv: heat
     capacity; dt: time step; inflow: {attribute: temperature} of isotropic
-    Planck inflow; T0: initial temperature (radiation in equilibrium with it)."""
+    Planck inflow; T0: initial temperature (radiation in equilibrium with it);
+    tune: pick the sweep's launch configuration with the autotuner first."""
 
     def __init__(self, mesh, order, quad, bounds, nu, opacity, cv, dt, T0, inflow=None, ac=1.0, c=1.0,
-                 method="fp64", tol=1e-8, inner_tol=1e-4, restart=30):
+                 method="fp64", tol=1e-8, inner_tol=1e-4, restart=30, tune=True):
         dev = torch.device("cuda")
         self.G = len(nu)
         self.nu = np.ascontiguousarray(nu, dtype=np.float64)
@@ -213,6 +214,9 @@ class LinearizedTRT:
         self.psi.view(G, self.Nw, Nd).copy_(torch.from_numpy(spec0).to(dev).view(G, 1, 1).expand(G, self.Nw, Nd))
         self.schur = TRTSchurOperator(self)
         self.steps = 0
+        if tune:   # schedule and threads per block of this handle's sweeps (results do not change)
+            from .autotune import autotune
+            self.tuned = autotune(self.L, reps=3, fp32=(method != "fp64"))
 
     def phi(self):
         """Scalar flux [G][Ndof] of the current psi."""

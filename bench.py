@@ -253,7 +253,9 @@ def trt_section(steps):
         psi_entries = s.L.width
         out[method] = {"seconds": secs, "ms_per_step": 1e3 * secs / steps, "krylov_iterations": int(np.sum(its)),
                        "max_iterations": int(np.max(its)), "fp64_sweeps": s64, "fp32_sweeps": s32, "converged": conv,
-                       "T_max": float(s.T.max().item())}
+                       "T_max": float(s.T.max().item()),
+                       "launch": {k: {kk: s.tuned[k][kk] for kk in ("schedule", "block")}
+                                  for k in ("fp64", "fp32") if k in s.tuned}}
         del s
         torch.cuda.empty_cache()
     out["psi_entries"] = psi_entries
