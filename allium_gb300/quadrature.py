@@ -20,6 +20,7 @@ set is the Gauss-Legendre rule with positive directions first
 """
 from __future__ import annotations
 
+import functools
 import math
 from dataclasses import dataclass
 
@@ -88,7 +89,9 @@ def _residual(N: int, mu1: float):
     return float(A[K] @ w - b[K]), w
 
 
+@functools.lru_cache(maxsize=None)
 def _solve_mu1(N: int) -> float:
+    """The first level of the LQn set (a scan and bisection; cached per N)."""
     if N == 2:
         return 1.0 / math.sqrt(3.0)
     lo_lim, hi_lim = 1e-3, 1.0 / math.sqrt(3.0) - 1e-9
