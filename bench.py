@@ -571,8 +571,11 @@ def run_gpu(args):
         L.Mult(hs, h_psi)
     barrier()
     t0 = time.perf_counter()
+    call_s = []
     for i in range(args.steps):
-        L.Mult(h_srcs[i % 2], h_psi)
+        tc = time.perf_counter()
+        L.Mult(h_srcs[i % 2], h_psi)   # returns with psi in host memory
+        call_s.append(time.perf_counter() - tc)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     e2e = world * N / e2e_s
     clk.__exit__(None, None, None)
@@ -603,6 +606,8 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(L.num_levels, cells),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
                     "ms_per_step": e2e_s * 1e3,
+                    "call_ms": {"median": 1e3 * float(np.median(call_s)), "min": 1e3 * min(call_s),
+                                "max": 1e3 * max(call_s)},
                     "pipeline": {"chunks": pipe["best"]["chunks"], "compute_streams": pipe["best"]["streams"],
                                  "taper": pipe["best"]["taper"],
                                  "trials_ms": {f"{t['chunks']}x{t['streams']}t{t['taper']}": round(t["ms"], 2)
