@@ -76,7 +76,7 @@ struct Handle {
     static constexpr int kMaxPipeStreams = 4;
     int pipe_chunks = 8;
     int pipe_streams = 4;
-    int pipe_taper = 1;
+    int pipe_taper = 0;
     int nchunk = 0;
     int chunk_taper = 0;
     std::vector<int> h_chunk_angle;   // [nchunk + 1] first angle of each chunk

@@ -147,7 +147,7 @@ class InverseAdvectionOperator:
         """Threads per block (32/64/128) of the FP64 (64) or FP32 (32) level kernels."""
         check(_lib.lib().allium_sweep_set_block_size(self.h, int(precision), int(threads)), self.h)
 
-    def SetPipeline(self, chunks, streams, taper=1):
+    def SetPipeline(self, chunks, streams, taper=0):
         """Direction slices (2..32), compute streams (1..4) and end-slice taper
         (0..3: first and last slices 1/2^taper of the others) of the
         pinned-host-buffer Mult."""

@@ -171,7 +171,7 @@ int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads);
  * swept and copied out on its own, and the sweeps of consecutive slices
  * alternate over `streams` compute streams (1..4).  With taper t (0..3) the
  * first and last slices get 1/2^t of the others' share of directions, which
- * shortens the pipeline's fill and drain.  Default 8, 4, 1.  No reference
+ * shortens the pipeline's fill and drain.  Default 8, 4, 0.  No reference
  * counterpart (the reference's vectors are host memory).  Results do not
  * depend on the shape. */
 int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int taper);
