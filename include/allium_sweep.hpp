@@ -113,6 +113,29 @@ public:
     void UseParallelBlockJacobi(bool use = true) { pbj_ = use; }
     bool IsParallelBlockJacobi() const { return pbj_; }
     void SetNumPBJSweeps(int n) { num_pbj_sweeps_ = n; }
+    // Exchange loads lagged off-rank traces for PBJ (src/sweep.cpp:877-922); one
+    // GPU owns every cell, so there is nothing to load.
+    void Exchange(const double* /*psi*/) {}
+    // message packing of the MPI sweep (src/sweep.hpp:109-110): no messages on one GPU
+    void SetSendBufferSize(int s) { send_buffer_size_ = s; }
+    void SetMaxSendsPerReceive(int s) { max_sends_per_recv_ = s; }
+
+    // Negative-flux fixup (src/sweep.hpp:112-118): kind 1 ZeroFixupOperator,
+    // 2 ZeroAndScaleFixupOperator (src/fixup.cpp:3-57), with its floor.
+    void SetFixupOperator(int kind, double minimum = 0.0) {
+        fix_kind_ = kind;
+        fix_min_ = minimum;
+        UseFixup(true);
+    }
+    void UseFixup(bool use = true) {
+        check(allium_sweep_set_fixup(h_, use ? fix_kind_ : 0, fix_min_), h_);
+        fix_on_ = use && fix_kind_ != 0;
+    }
+    bool IsFixupOn() const { return fix_on_; }
+    // local solves the fixup changed / could not balance since the last reset
+    void FixupCounts(long long* applied, long long* failed, bool reset = false) const {
+        check(allium_sweep_fixup_counts(h_, applied, failed, reset ? 1 : 0), h_);
+    }
     void Synchronize() const { check(allium_sweep_synchronize(h_), h_); }
 
     allium_sweep* handle() const { return h_; }
@@ -124,6 +147,10 @@ private:
     double tau_ = 0.0;
     bool pbj_ = false;
     int num_pbj_sweeps_ = 1;
+    int send_buffer_size_ = 8, max_sends_per_recv_ = 8;
+    int fix_kind_ = 0;
+    double fix_min_ = 0.0;
+    bool fix_on_ = false;
 };
 
 // AdvectionOperator (src/sweep.hpp:155-166)

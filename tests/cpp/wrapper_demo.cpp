@@ -52,6 +52,19 @@ int main() {
     std::vector<double> phi(Linv.NumDofs());
     D.Mult(psi.data(), phi.data());
     for (double x : phi) err = std::fmax(err, std::fabs(x / (4 * M_PI) - 1.0));
+    // the reference's fixup and PBJ controls (src/sweep.hpp:100-118): with no
+    // negative flux the zero fixup changes nothing and counts no application
+    Linv.UseParallelBlockJacobi(true);
+    Linv.SetNumPBJSweeps(2);
+    Linv.Exchange(psi.data());
+    Linv.SetFixupOperator(1);
+    if (!Linv.IsFixupOn()) return 2;
+    Linv.Mult(source.data(), psi.data());
+    long long applied = -1, failed = -1;
+    Linv.FixupCounts(&applied, &failed, true);
+    for (double x : psi) err = std::fmax(err, std::fabs(x - 1.0));
+    Linv.UseFixup(false);
+    if (Linv.IsFixupOn() || applied != 0 || failed != 0) return 3;
     std::printf("ok %.3e levels %d\n", err, Linv.NumLevels());
     return err < 1e-10 ? 0 : 1;
 }
