@@ -50,6 +50,7 @@ EXPORTS = {
     "allium_sweep_set_fixup": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "allium_sweep_set_block_size": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "allium_sweep_set_pipeline": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "allium_sweep_set_f32_inverse_layout": (C.c_int, [C.c_void_p, C.c_int]),
     "allium_sweep_relayout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "allium_sweep_fixup_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.c_int]),
     "allium_sweep_apply_L": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

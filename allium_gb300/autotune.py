@@ -3,7 +3,8 @@
 The knobs are the schedule (wavefront levels, one launch per level captured
 in a CUDA graph, or the persistent dataflow kernel with per-node completion
 flags) and the threads per block of the thread-per-node level kernels, for
-the FP64 sweep and the FP32 sweep (node-major layout) separately, and the
+the FP64 sweep and the FP32 sweep (node-major layout) separately, the order
+of the FP32 inverse copy that the node-major sweep reads, and the
 shape of the pinned-host-buffer pipeline (direction slices, compute streams).  Each
 candidate is timed with CUDA events over a few Mults after one untimed call
 (which captures its graph and, for FP64, builds the factor cache once), the
@@ -56,12 +57,15 @@ def autotune(L, reps=3, blocks=(32, 64, 128), fp32=True, schedules=None):
         L.ToNodeLayoutF32(src, f)
         g = torch.empty_like(f)
         best32 = None
-        for b in blocks:
-            L.SetBlockSize(32, b)
-            ms = _time(lambda: L.MultF32Nodes(f, g), reps)
-            trials.append({"precision": 32, "schedule": best["schedule"], "block": b, "ms": ms})
-            if best32 is None or ms < best32["ms"]:
-                best32 = trials[-1]
+        for layout in (0, 1):
+            L.SetF32InverseLayout(layout)
+            for b in blocks:
+                L.SetBlockSize(32, b)
+                ms = _time(lambda: L.MultF32Nodes(f, g), reps)
+                trials.append({"precision": 32, "schedule": best["schedule"], "block": b, "layout": layout, "ms": ms})
+                if best32 is None or ms < best32["ms"]:
+                    best32 = trials[-1]
+        L.SetF32InverseLayout(best32["layout"])
         L.SetBlockSize(32, best32["block"])
         out["fp32"] = best32
     L.synchronize()

@@ -686,6 +686,18 @@ int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads) {
     return ALLIUM_OK;
 }
 
+int allium_sweep_set_f32_inverse_layout(allium_sweep* s, int entry_major) {
+    if (!s || (entry_major != 0 && entry_major != 1)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (h.f_inv_entry_major != entry_major) {
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h.stream));
+        h.f_inv_entry_major = entry_major;
+        h.f_inv_valid = false;   // rewritten in the new order on the next node-layout sweep
+        allium::drop_graphs(h);
+    }
+    return ALLIUM_OK;
+}
+
 int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int taper) {
     if (!s || chunks < 2 || chunks > allium::Handle::kMaxPipeChunks || streams < 1 ||
         streams > allium::Handle::kMaxPipeStreams || taper < 0 || taper > 3)

@@ -110,6 +110,7 @@ struct Handle {
     float* f_inv_nodes = nullptr;
     bool f_inv_valid = false;
     bool f_inv_failed = false;        // the copy did not fit: recompute instead
+    int f_inv_entry_major = 0;        // 1: entry (i, j) of node-group t at [(i n + j) * total + t]
 
     // CUDA graphs of the per-level launch sequence, keyed by kind and vectors
     struct GraphEntry {

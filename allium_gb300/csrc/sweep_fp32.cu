@@ -44,8 +44,13 @@ cudaError_t sweep_levels_nodes_cached(Handle& h, const SweepArgs<float>& args, c
         const long long threads = (long long)count * h.G;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_nodes_cached<D, P><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, h.f_inv_nodes,
-                                                                (long long)off * h.G);
+        const long long stride = (long long)h.G * h.ne * h.Nw;
+        if (h.f_inv_entry_major)
+            k_sweep_nodes_cached<D, P, true><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count,
+                                                                          h.f_inv_nodes, (long long)off * h.G, stride);
+        else
+            k_sweep_nodes_cached<D, P, false><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count,
+                                                                           h.f_inv_nodes, (long long)off * h.G, stride);
     }
     return cudaGetLastError();
 }
@@ -68,6 +73,13 @@ static bool ensure_f32_inverses(Handle& h) {
             h.f_inv_failed = true;
             return false;
         }
+    }
+    if (h.f_inv_entry_major) {
+        const long long n = total * NN;
+        k_inv_to_f32_entries<<<(unsigned)((n + 255) / 256), 256, 0, h.stream>>>(n, h.d_inv, h.f_inv_nodes);
+        if (cudaGetLastError() != cudaSuccess) return false;
+        h.f_inv_valid = true;
+        return true;
     }
     const long long work = total * h.n;
     const unsigned grid = (unsigned)((work + 255) / 256);

@@ -878,12 +878,21 @@ __global__ void k_inv_to_f32(long long total, long long stride, const double* __
     store_block<N>(out + (t * N + i) * N, row);
 }
 
+// The FP64 inverses' entry-major order kept in FP32: out[e * total + t] =
+// inv64[e * total + t] for the N*N entries e (one warp load = 32 nodes' entry).
+static __global__ void k_inv_to_f32_entries(long long n, const double* __restrict__ inv64, float* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < n) out[idx] = (float)inv64[idx];
+}
+
 // Node-major FP32 sweep from the stored FP32 inverses: right-hand side as in
-// k_sweep_nodes, then psi = inv(A) b with the node's inverse read as float4 rows.
-template <int D, int P>
+// k_sweep_nodes, then psi = inv(A) b.  ENTRY_MAJOR: entry (i, j) of node-group
+// t at inv[(i N + j) stride + t] (coalesced across a warp); otherwise each
+// node-group's N x N block is contiguous and read as float4 rows.
+template <int D, int P, bool ENTRY_MAJOR = false>
 __global__ void __launch_bounds__(128) k_sweep_nodes_cached(SweepArgs<float> s, const int* __restrict__ nodes,
                                                             int count, const float* __restrict__ inv,
-                                                            long long base) {
+                                                            long long base, long long stride) {
     constexpr int N = ipow(P + 1, D);
     constexpr int NF = ipow(P + 1, D - 1);
     constexpr int NFACE = 2 * D;
@@ -928,16 +937,27 @@ __global__ void __launch_bounds__(128) k_sweep_nodes_cached(SweepArgs<float> s, 
             }
         }
     }
-    const float* in = inv + (base + t) * (long long)(N * N);
     float x[N];
+    if constexpr (ENTRY_MAJOR) {
+        const float* in = inv + base + t;
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-        float row[N];
-        load_block<N>(in + i * N, row);
-        float acc = 0.0f;
+        for (int i = 0; i < N; ++i) {
+            float acc = 0.0f;
 #pragma unroll
-        for (int j = 0; j < N; ++j) acc = fmaf(row[j], b[j], acc);
-        x[i] = acc;
+            for (int j = 0; j < N; ++j) acc = fmaf(__ldg(in + (long long)(i * N + j) * stride), b[j], acc);
+            x[i] = acc;
+        }
+    } else {
+        const float* in = inv + (base + t) * (long long)(N * N);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            float row[N];
+            load_block<N>(in + i * N, row);
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < N; ++j) acc = fmaf(row[j], b[j], acc);
+            x[i] = acc;
+        }
     }
     store_block<N>(s.psi + node_index(s.Nw, s.G, N, e, a, g), x);
 }

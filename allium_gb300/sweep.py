@@ -153,6 +153,10 @@ class InverseAdvectionOperator:
         pinned-host-buffer Mult."""
         check(_lib.lib().allium_sweep_set_pipeline(self.h, int(chunks), int(streams), int(taper)), self.h)
 
+    def SetF32InverseLayout(self, entry_major):
+        """Order of the FP32 inverse copy of the node-major FP32 sweep: 0 block per node-group, 1 entry-major."""
+        check(_lib.lib().allium_sweep_set_f32_inverse_layout(self.h, int(entry_major)), self.h)
+
     def SetFactorCache(self, mode):
         """1: keep FP64 local-matrix inverses across Mults when memory allows (default); 0: off."""
         check(_lib.lib().allium_sweep_set_factor_cache(self.h, int(mode)), self.h)

@@ -165,6 +165,13 @@ int allium_sweep_mult_f32(allium_sweep* s, const float* source, float* psi);
  * reference counterpart).  Default 128. */
 int allium_sweep_set_block_size(allium_sweep* s, int precision, int threads);
 
+/* Order of the FP32 copy of the stored inverses that the node-major FP32 sweep
+ * reads: 0 each node-group's n x n block contiguous (float4 rows, default),
+ * 1 entry-major like the FP64 store (one warp load = one entry of 32
+ * node-groups).  A tuning knob with no reference counterpart; results do not
+ * depend on it. */
+int allium_sweep_set_f32_inverse_layout(allium_sweep* s, int entry_major);
+
 /* Shape of the host-buffer pipeline of allium_sweep_mult (pinned host vectors,
  * stored inverses, inflow boundaries): the directions are cut into `chunks`
  * contiguous slices (2..32, at most half the directions), each copied in,

@@ -505,6 +505,31 @@ def test_autotune_keeps_results():
 
 
 @pytest.mark.parametrize("dim,cells,sn,G", [(3, (6, 5, 4), 6, 2), (2, (12, 9), 8, 3)])
+def test_f32_inverse_layouts(dim, cells, sn, G):
+    # both orders of the FP32 inverse copy give the same node-major FP32 sweep,
+    # within the FP32 tolerance of the oracle
+    mesh, quad, sig, o, L = build(dim, cells, 1, sn, G, 0.1, 0)
+    src = np.random.default_rng(2).random(o.psi_size)
+    ref = o.mult(src)
+    f = torch.empty(L.width, dtype=torch.float32, device="cuda")
+    out = {}
+    for layout in (1, 0, 1):
+        L.SetF32InverseLayout(layout)
+        L.ToNodeLayoutF32(torch.from_numpy(src).cuda(), f)
+        L.MultF32Nodes(f, f)
+        back = torch.empty(L.width, dtype=torch.float64, device="cuda")
+        L.FromNodeLayoutF32(f, back)
+        L.synchronize()
+        assert rel_err(back.cpu().numpy(), ref) < TOL32
+        if layout in out:
+            assert torch.equal(back, out[layout])
+        out[layout] = back
+    assert torch.equal(out[0], out[1])
+    with pytest.raises(AlliumError):
+        L.SetF32InverseLayout(2)
+
+
+@pytest.mark.parametrize("dim,cells,sn,G", [(3, (6, 5, 4), 6, 2), (2, (12, 9), 8, 3)])
 def test_pinned_host_mult_pipeline(dim, cells, sn, G):
     # page-locked host vectors take the chunked copy/sweep/copy pipeline; every
     # node is computed with the same arithmetic, so psi matches the device Mult
