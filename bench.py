@@ -146,13 +146,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sweep_sample(threads, steps, warmup):
-    """CPU restatement of Mult_Upwind (OpenMP) on the workload mesh with 8 of
-    the 168 directions (one per octant).  Returns DOF*angle*group/s per step."""
+def cpu_sweep_sample(threads, steps, warmup, ndir=8):
+    """CPU restatement of Mult_Upwind (OpenMP) on the workload mesh with ndir of
+    the 168 directions (one per octant for ndir = 8).  Returns DOF*angle*group/s
+    per step."""
     from oracle.oracle import OracleSweep
     from allium_gb300 import quadrature as Q
     mesh, quad, sigma, q = workload()
-    pick = [i * (quad.size // 8) for i in range(8)]
+    pick = [i * (quad.size // 8) for i in range(ndir)]
     sub = Q.AngularQuadrature(3, quad.omega[pick].copy(), quad.weights[pick].copy())
     o = OracleSweep(mesh, ORDER, sub, sigma)
     src = o.form_source(q_cell=q)
@@ -620,6 +621,15 @@ def run_gpu(args):
             "fp64_pipe": {"achieved_gdfma_s": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9,
                           "peak_gdfma_s": 625.0, "peak_kind": "nominal",
                           "frac": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9 / 625.0},
+            # the same bound in the units of a flop roofline: flops executed per DOF*angle
+            # (2 per DFMA) against the reference algorithm's (per-node assembly and LU,
+            # about 211 for 3D p = 1), whose work the stored inverses avoid
+            "compute_roofline": {"executed_flops_per_unit": 2.0 * (64 + 3 * 20) / 8,
+                                 "reference_algorithm_flops_per_unit": 211,
+                                 "achieved_tflops": N * 2.0 * (64 + 3 * 20) / 8 / (ms * 1e-3) / 1e12,
+                                 "peak_tflops": 1.25, "peak_kind": "nominal FP64",
+                                 "frac": N * 2.0 * (64 + 3 * 20) / 8 / (ms * 1e-3) / 1e12 / 1.25,
+                                 "reference_algorithm_equivalent_tflops": N * 211 / (ms * 1e-3) / 1e12},
             "fp64_uncached": {"value": N / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                               "note": "every Mult assembles and factors all local systems (pivoted LU), as the reference does"},
             "fp64_first_mult_ms": ms_first,
@@ -649,6 +659,9 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": statistics.median(rates), "unit": UNIT, "cores": os.cpu_count(),
                                 "kind": "port",
                                 "sample": f"full 64^3 mesh, 8 of 168 S12 directions (one per octant), {size} DOF*angle per sweep, median of 3"}
+        rates1, size1 = cpu_sweep_sample(1, 3, 1, ndir=1)
+        line["cpu_baseline_1thread"] = {"value": statistics.median(rates1), "unit": UNIT, "cores": 1, "kind": "port",
+                                        "sample": f"full 64^3 mesh, 1 of 168 S12 directions, {size1} DOF*angle per sweep, median of 3"}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
