@@ -55,6 +55,10 @@ int check_status(Handle& h) {
         CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_status, 0, sizeof(int), h.stream));
         if (st & allium::kErrSingular) { h.last_error = "zero pivot in a local solve"; return ALLIUM_ERR_SINGULAR; }
         if (st & allium::kErrTimeout) { h.last_error = "a bounded device wait gave up"; return ALLIUM_ERR_TIMEOUT; }
+        if (st & allium::kErrFixup) {
+            h.last_error = "Ryosuke fixup with more than three positive entries (src/fixup.cpp:155 aborts)";
+            return ALLIUM_ERR_UNSUPPORTED;
+        }
         h.last_error = "non-finite value";
         return ALLIUM_ERR_NAN;
     }
@@ -711,7 +715,7 @@ int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int tape
 int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum) {
     if (!s || kind < 0) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
-    if (kind > 2) { h.last_error = "only the zero (1) and zero-and-scale (2) fixups are implemented"; return ALLIUM_ERR_UNSUPPORTED; }
+    if (kind > 4) { h.last_error = "fixup kinds: 1 zero, 2 zero and scale, 3 Ryosuke, 4 local optimization"; return ALLIUM_ERR_UNSUPPORTED; }
     if (kind && h.n > 8) { h.last_error = "the fixup is implemented for local systems up to 8 x 8"; return ALLIUM_ERR_UNSUPPORTED; }
     if (!h.d_fix_counts) {
         CUDA_OR_FAIL(h, cudaMalloc(&h.d_fix_counts, 2 * sizeof(unsigned long long)));

@@ -202,6 +202,7 @@ inline void drop_graphs(Handle& h) {
 constexpr int kErrSingular = 1;
 constexpr int kErrNaN = 2;
 constexpr int kErrTimeout = 4;
+constexpr int kErrFixup = 8;     // Ryosuke fixup with more than three positive entries
 // node-groups per tile of the dataflow schedule (= threads per block)
 constexpr int kTile = 128;
 

@@ -46,11 +46,108 @@ struct SweepArgs {
     unsigned long long* fix_counts;   // [0] applied, [1] failed
 };
 
-// ZeroFixupOperator / ZeroAndScaleFixupOperator::Apply (src/fixup.cpp:3-57) on
-// the solved local vector x, with w the column sums of the local matrix and
-// balance = sum of the right-hand side.  Returns 0 (untouched), 1 or -1.
+// RyosukeFixupOperator::Apply / perform_nff (src/fixup.cpp:90-174): negative entries
+// to the floor, then the remaining ("positive") entries rescaled so that
+// w . x equals the source total, by the reference's closed forms for 1, 2 or 3
+// positive entries.  Returns 0, 1, -1, or -2 for more than three positive
+// entries (where the reference aborts, src/fixup.cpp:155).
+template <int N, typename R>
+__device__ __noinline__ int fixup_ryosuke(R xmin, const R (&w)[N], R balance, R (&x)[N]) {
+    int cnt[N];
+    int pos = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if (x[i] <= xmin) x[i] = xmin;
+        else cnt[pos++] = i;
+    }
+    if (pos == 0 || pos == N) return 0;
+    if (pos > 3) return -2;
+    R xv[3], wv[3];
+    for (int k = 0; k < pos; ++k) {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (i == cnt[k]) { xv[k] = x[i]; wv[k] = w[i]; }
+    }
+    // C: first row the weights of the positive entries, first column
+    // -x_k / x_0 below the diagonal of ones; right-hand side (balance, 0, ..)
+    R out[3];
+    if (pos == 1) {
+        out[0] = balance / wv[0];
+    } else if (pos == 2) {
+        const R c0 = wv[0], c1 = wv[1], c2 = -xv[1] / xv[0], c3 = R(1);
+        R det = c0 * c3 - c1 * c2;
+        det = R(1) / det;
+        out[0] = balance * c3 * det;
+        out[1] = -balance * c2 * det;
+    } else {
+        const R c0 = wv[0], c1 = wv[1], c2 = wv[2];
+        const R c3 = -xv[1] / xv[0], c4 = R(1), c6 = -xv[2] / xv[0], c8 = R(1);
+        R det = c0 * c4 * c8 - c1 * c3 * c8 - c2 * c4 * c6;
+        det = R(1) / det;
+        out[0] = balance * c4 * c8 * det;
+        out[1] = -balance * c3 * c8 * det;
+        out[2] = -balance * c4 * c6 * det;
+    }
+    bool fail = false;
+    for (int k = 0; k < pos; ++k) fail = fail || out[k] < xmin;
+    for (int k = 0; k < pos; ++k) {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (i == cnt[k]) x[i] = fail ? xmin : out[k];
+    }
+    return fail ? -1 : 1;
+}
+
+// LocalOptimizationFixupOperator::Apply (src/fixup.cpp:59-88): the point
+// nearest to the solved x0 with w . x = source total and x >= floor, the
+// problem mfem::SLBQPOptimizer solves iteratively (to 1e-12 relative in
+// allium's setup, src/io.cpp:879-890).  Here exactly: x_i = max(x0_i +
+// lam w_i, floor) with lam from the active set, shrunk until no free entry
+// falls below the floor (each pass lowers lam, so a clamped entry stays
+// clamped; at most N passes).  Entries with w_i = 0 take max(x0_i, floor).
+template <int N, typename R>
+__device__ __noinline__ int fixup_local_optimization(R xmin, const R (&w)[N], R balance, R (&x)[N]) {
+    R lo = x[0];
+#pragma unroll
+    for (int i = 1; i < N; ++i) lo = x[i] < lo ? x[i] : lo;
+    if (lo > xmin || balance <= xmin) return 0;
+    bool freev[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) freev[i] = w[i] > R(0);
+    R lam = R(0);
+    bool feasible = false;
+    for (int pass = 0; pass <= N; ++pass) {
+        R rest = balance, ww = R(0);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            if (freev[i]) { rest -= w[i] * x[i]; ww += w[i] * w[i]; }
+            else rest -= w[i] * (x[i] > xmin ? x[i] : xmin);
+        }
+        if (!(ww > R(0))) break;
+        lam = rest / ww;
+        bool clamped = false;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (freev[i] && x[i] + lam * w[i] < xmin) { freev[i] = false; clamped = true; }
+        if (!clamped) { feasible = true; break; }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const R v = freev[i] && feasible ? x[i] + lam * w[i] : x[i];
+        x[i] = v > xmin ? v : xmin;
+    }
+    return feasible ? 1 : -1;
+}
+
+// ZeroFixupOperator / ZeroAndScaleFixupOperator::Apply (src/fixup.cpp:3-57),
+// kinds 1 and 2, and the Ryosuke (3) and local-optimization (4) fixups above,
+// on the solved local vector x, with w the column sums of the local matrix and
+// balance = sum of the right-hand side.  Returns 0 (untouched), 1, -1, or -2
+// (Ryosuke with more than three positive entries).
 template <int N, typename R>
 __device__ __forceinline__ int apply_fixup(int kind, R xmin, const R (&w)[N], R balance, R (&x)[N]) {
+    if (kind == 3) return fixup_ryosuke<N, R>(xmin, w, balance, x);
+    if (kind == 4) return fixup_local_optimization<N, R>(xmin, w, balance, x);
     R lo = x[0];
 #pragma unroll
     for (int i = 1; i < N; ++i) lo = x[i] < lo ? x[i] : lo;
@@ -425,6 +522,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 4 : 1)) k_sweep_level(S
     if (!solve_local<N, PIVOT>(A, b)) atomicOr(s.status, kErrSingular);
     if (s.fix_kind) {
         const int r = apply_fixup<N, R>(s.fix_kind, s.fix_min, w, balance, b);
+        if (r == -2) atomicOr(s.status, kErrFixup);
         if (r) atomicAdd(s.fix_counts + (r > 0 ? 0 : 1), 1ull);
     }
     store_block<N>(s.psi + psi_index(s.ndof, s.Nw, g, a, (long long)e * N), b);

@@ -186,8 +186,11 @@ int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int tape
 /* Negative-flux fixup inside the sweep (SetFixupOperator / UseFixup,
  * src/sweep.hpp:108-117, applied at src/sweep.cpp:465-470): kind 0 off,
  * 1 ZeroFixupOperator, 2 ZeroAndScaleFixupOperator (src/fixup.cpp:3-57),
- * with the operator's minimum_solution.  The local-optimization and
- * "Ryosuke" fixups return ALLIUM_ERR_UNSUPPORTED, as do systems above 8 x 8.
+ * 3 RyosukeFixupOperator (src/fixup.cpp:90-174), 4 LocalOptimizationFixupOperator
+ * (src/fixup.cpp:59-88; the bound-constrained projection solved exactly instead of
+ * by mfem::SLBQPOptimizer's iteration), with the operator's minimum_solution.
+ * Where the reference aborts (Ryosuke with more than three positive entries) the
+ * sweep returns ALLIUM_ERR_UNSUPPORTED; systems above 8 x 8 are refused.
  * While a fixup is on, Mult rebuilds and factors every local system. */
 int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum);
 

@@ -52,6 +52,8 @@ def lib():
         L.oracle_absorption.argtypes = [vp, dp, dp, dp]
         L.oracle_powerlaw_opacity.argtypes = [vp, dp, dp, C.c_double, C.c_double, C.c_double, dp]
         L.oracle_fixup_counts.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.oracle_fixup_unsupported.argtypes = [vp]
+        L.oracle_fixup_unsupported.restype = C.c_longlong
         L.oracle_scattering_source.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_l2_error.argtypes = [vp, dp, C.c_int, C.c_int, FN]
         L.oracle_l2_error.restype = C.c_double
@@ -196,6 +198,10 @@ class OracleSweep:
         a, f = C.c_longlong(), C.c_longlong()
         lib().oracle_fixup_counts(self.h, C.byref(a), C.byref(f))
         return a.value, f.value
+
+    def fixup_unsupported(self):
+        """Ryosuke solves with more than three positive entries (the reference aborts there)."""
+        return lib().oracle_fixup_unsupported(self.h)
 
     def levels(self):
         lev = np.zeros(self.ne * self.Nw, dtype=np.int32)

@@ -24,7 +24,7 @@
 //                           moments phi(g,m,i) = i + Ndof*(g + G*m)
 //   src/sweep.cpp:177-195,432-437, src/angular_quadrature.cpp:8-36
 //                           reflective boundaries (mirror angle edges and trace)
-//   src/fixup.cpp:3-57      zero / zero-and-scale negative-flux fixups
+//   src/fixup.cpp:3-174     zero, zero-and-scale, local-optimization and Ryosuke negative-flux fixups
 //   src/planck.hpp:157-236  Planck / Rosseland group integrals
 //   src/trt_integrators.cpp:56-302, exe/scallion.cpp:755-797,1352-1470,
 //   src/tvector.cpp:76-95   TRT emission, energy balance, absorption, time source
@@ -161,6 +161,7 @@ struct Oracle {
     std::vector<double> sigma;  // [G][ne]
     bool timedep = false; double tau = 0.0;
     int fix_kind = 0; double fix_min = 0.0;        // negative-flux fixup (fixup.cpp)
+    long long fix_unsupported = 0;                  // Ryosuke solves with more than three positive entries
     long long fix_applied = 0, fix_failed = 0;
     std::vector<double> basis_nodes;
     std::vector<double> Ms, Gm, Mt, F;  // see assemble()
@@ -525,6 +526,87 @@ bool lu_solve(int m, double* A, double* x) {
 }
 
 // mfem::LinearSolve restated: closed forms for n = 1, 2; LU otherwise
+// RyosukeFixupOperator::perform_nff (src/fixup.cpp:96-174): entries at or
+// below the floor set to it; the others ("positive") solve C y = d with C's
+// first row the column sums w of the positive entries, its first column
+// -x_k / x_0 below a unit diagonal, d = (sum b, 0, ...), in the reference's
+// closed forms for 1, 2, 3 unknowns.  -2 where the reference aborts (more
+// than three positive entries).
+int fixup_ryosuke(int n, const double* w, double total, double* x, double xmin) {
+    std::vector<int> count;
+    for (int i = 0; i < n; ++i) {
+        if (x[i] <= xmin) x[i] = xmin;
+        else count.push_back(i);
+    }
+    const int pos = (int)count.size();
+    if (pos == 0 || pos == n) return 0;
+    if (pos > 3) return -2;
+    std::vector<double> C((size_t)pos * pos, 0.0);
+    for (int i = 0; i < pos; ++i) {
+        C[i] = w[count[i]];
+        if (i == 0) {
+            for (int j = 1; j < pos; ++j) C[(size_t)j * pos] = -x[count[j]] / x[count[0]];
+        } else {
+            C[(size_t)i * (pos + 1)] = 1.0;
+        }
+    }
+    const double d0 = total;
+    if (pos == 1) {
+        x[count[0]] = d0 / C[0];
+    } else if (pos == 2) {
+        double det = C[0] * C[3] - C[1] * C[2];
+        det = 1.0 / det;
+        x[count[0]] = d0 * C[3] * det;
+        x[count[1]] = -d0 * C[2] * det;
+    } else {
+        double det = C[0] * C[4] * C[8] - C[1] * C[3] * C[8] - C[2] * C[4] * C[6];
+        det = 1.0 / det;
+        x[count[0]] = d0 * C[4] * C[8] * det;
+        x[count[1]] = -d0 * C[3] * C[8] * det;
+        x[count[2]] = -d0 * C[4] * C[6] * det;
+    }
+    for (int k = 0; k < pos; ++k)
+        if (x[count[k]] < xmin) {
+            for (int j = 0; j < pos; ++j) x[count[j]] = xmin;
+            return -1;
+        }
+    return 1;
+}
+
+// LocalOptimizationFixupOperator::Apply (src/fixup.cpp:59-88): argmin
+// |x - x0|^2 subject to w . x = sum b and x >= floor (what
+// mfem::SLBQPOptimizer iterates towards).  The minimiser is
+// x_i = max(x0_i + lam w_i, floor); lam is found exactly by clamping every
+// free entry that falls below the floor and recomputing lam on the rest, until
+// none does.  Entries with w_i = 0 take max(x0_i, floor).
+int fixup_local_opt(int n, const double* w, double total, double* x, double xmin) {
+    double lo = x[0];
+    for (int i = 1; i < n; ++i) lo = std::min(lo, x[i]);
+    if (lo > xmin || total <= xmin) return 0;
+    std::vector<char> freev(n);
+    for (int i = 0; i < n; ++i) freev[i] = w[i] > 0.0;
+    double lam = 0.0;
+    bool feasible = false;
+    for (int pass = 0; pass <= n; ++pass) {
+        double rest = total, ww = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (freev[i]) { rest -= w[i] * x[i]; ww += w[i] * w[i]; }
+            else rest -= w[i] * (x[i] > xmin ? x[i] : xmin);
+        }
+        if (!(ww > 0.0)) break;
+        lam = rest / ww;
+        bool clamped = false;
+        for (int i = 0; i < n; ++i)
+            if (freev[i] && x[i] + lam * w[i] < xmin) { freev[i] = 0; clamped = true; }
+        if (!clamped) { feasible = true; break; }
+    }
+    for (int i = 0; i < n; ++i) {
+        const double v = freev[i] && feasible ? x[i] + lam * w[i] : x[i];
+        x[i] = v > xmin ? v : xmin;
+    }
+    return feasible ? 1 : -1;
+}
+
 bool linear_solve(int m, double* A /*column major*/, double* x) {
     if (m == 1) { if (A[0] == 0.0) return false; x[0] /= A[0]; return true; }
     if (m == 2) {
@@ -616,6 +698,18 @@ bool solve_node(const Oracle& o, int e, int a, const double* src, double* psi,
             for (int i = 1; i < n; ++i) lo = std::min(lo, rhs[i]);
             if (o.fix_kind == 1) {
                 for (int i = 0; i < n; ++i) if (rhs[i] <= o.fix_min) { rhs[i] = o.fix_min; applied = 1; }
+            } else if (o.fix_kind == 3 || o.fix_kind == 4) {
+                std::vector<double> w(n, 0.0);
+                for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) w[i] += Acopy[j + i * n];
+                double total = 0.0;
+                for (int i = 0; i < n; ++i) total += bcopy[i];
+                applied = o.fix_kind == 3 ? fixup_ryosuke(n, w.data(), total, rhs.data(), o.fix_min)
+                                          : fixup_local_opt(n, w.data(), total, rhs.data(), o.fix_min);
+                if (applied == -2) {
+#pragma omp atomic
+                    const_cast<Oracle&>(o).fix_unsupported += 1;
+                    applied = -1;
+                }
             } else if (!(lo > o.fix_min)) {
                 std::vector<double> w(n, 0.0);
                 for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) w[i] += Acopy[j + i * n];
@@ -707,8 +801,10 @@ int oracle_set_reflective(void* h, int num, const int* attrs) {
 
 void oracle_set_fixup(void* h, int kind, double minimum) {
     Oracle& o = *static_cast<Oracle*>(h);
-    o.fix_kind = kind; o.fix_min = minimum; o.fix_applied = o.fix_failed = 0;
+    o.fix_kind = kind; o.fix_min = minimum; o.fix_applied = o.fix_failed = 0; o.fix_unsupported = 0;
 }
+
+long long oracle_fixup_unsupported(void* h) { return static_cast<Oracle*>(h)->fix_unsupported; }
 
 void oracle_fixup_counts(void* h, long long* applied, long long* failed) {
     const Oracle& o = *static_cast<Oracle*>(h);

@@ -332,10 +332,11 @@ def test_bounded_wait_reports_timeout():
 
 
 @pytest.mark.parametrize("dim,cells", [(2, (16, 16)), (3, (8, 8, 8))])
-@pytest.mark.parametrize("kind", [1, 2])
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
 def test_fixup_parity(dim, cells, kind):
     # optically thick cells next to a point source: p = 1 DG fluxes dip below
-    # zero; the zero (1) and zero-and-scale (2) fixups of src/fixup.cpp remove them
+    # zero; the zero (1), zero-and-scale (2), Ryosuke (3) and local-optimization
+    # (4) fixups of src/fixup.cpp remove them
     mesh = M.cartesian(cells, jitter=0.1, seed=2)
     quad = Q.level_symmetric(4, dim)
     sig = np.full((2, mesh.num_elements), 50.0)
@@ -352,12 +353,21 @@ def test_fixup_parity(dim, cells, kind):
     L.SetFixup(kind, 0.0)
     ref = o.mult(src)
     psi = np.empty_like(src)
+    if o.fixup_unsupported():
+        # Ryosuke with more than three positive entries: the reference aborts
+        with pytest.raises(AlliumError) as e:
+            L.Mult(src, psi)
+        assert e.value.status == 7
+        L.SetFixup(0)
+        return
     L.Mult(src, psi)
     assert psi.min() >= 0.0
     assert rel_err(psi, ref) < 1e-11
+    if kind >= 2 and o.fixup_counts()[1] == 0:   # the conservative fixups keep the balance
+        assert abs(AdvectionOperator(L).ComputeBalance(psi) - o.balance(plain)) < 1e-9 * abs(o.balance(plain))
     applied, failed = L.FixupCounts(reset=True)
     ra, rf = o.fixup_counts()
-    assert abs(applied - ra) <= max(3, ra // 100) and failed == rf
+    assert abs(applied - ra) <= max(3, ra // 100) and abs(failed - rf) <= max(3, rf // 100)
     f32 = torch.from_numpy(src.astype(np.float32)).cuda()
     L.MultF32(f32, f32)
     L.synchronize()
