@@ -716,7 +716,6 @@ int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum) {
     if (!s || kind < 0) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
     if (kind > 4) { h.last_error = "fixup kinds: 1 zero, 2 zero and scale, 3 Ryosuke, 4 local optimization"; return ALLIUM_ERR_UNSUPPORTED; }
-    if (kind && h.n > 8) { h.last_error = "the fixup is implemented for local systems up to 8 x 8"; return ALLIUM_ERR_UNSUPPORTED; }
     if (!h.d_fix_counts) {
         CUDA_OR_FAIL(h, cudaMalloc(&h.d_fix_counts, 2 * sizeof(unsigned long long)));
         CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_fix_counts, 0, 2 * sizeof(unsigned long long), h.stream));

@@ -117,11 +117,13 @@ __device__ __noinline__ int fixup_local_optimization(R xmin, const R (&w)[N], R 
     R lam = R(0);
     bool feasible = false;
     for (int pass = 0; pass <= N; ++pass) {
+        // free entries contribute w (x0 + lam w), clamped ones w * floor,
+        // entries with w = 0 nothing
         R rest = balance, ww = R(0);
 #pragma unroll
         for (int i = 0; i < N; ++i) {
             if (freev[i]) { rest -= w[i] * x[i]; ww += w[i] * w[i]; }
-            else rest -= w[i] * (x[i] > xmin ? x[i] : xmin);
+            else if (w[i] > R(0)) rest -= w[i] * xmin;
         }
         if (!(ww > R(0))) break;
         lam = rest / ww;
@@ -131,12 +133,17 @@ __device__ __noinline__ int fixup_local_optimization(R xmin, const R (&w)[N], R 
             if (freev[i] && x[i] + lam * w[i] < xmin) { freev[i] = false; clamped = true; }
         if (!clamped) { feasible = true; break; }
     }
+    if (!feasible) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = x[i] > xmin ? x[i] : xmin;
+        return -1;
+    }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-        const R v = freev[i] && feasible ? x[i] + lam * w[i] : x[i];
+        const R v = freev[i] ? x[i] + lam * w[i] : (w[i] > R(0) ? xmin : x[i]);
         x[i] = v > xmin ? v : xmin;
     }
-    return feasible ? 1 : -1;
+    return 1;
 }
 
 // ZeroFixupOperator / ZeroAndScaleFixupOperator::Apply (src/fixup.cpp:3-57),
@@ -175,6 +182,20 @@ __device__ __forceinline__ int apply_fixup(int kind, R xmin, const R (&w)[N], R 
         for (int i = 0; i < N; ++i) x[i] *= sc;
     }
     return 1;
+}
+
+// The fixup on a solution and column sums held in shared (or any) memory, out
+// of line so that the team and block kernels keep their register budget for
+// the fixup-free path; counts and the Ryosuke abort status recorded here.
+template <int N, typename R>
+__device__ __noinline__ void apply_fixup_mem(int kind, R xmin, R* xs, const R* ws, R balance, int* status,
+                                             unsigned long long* counts) {
+    R x[N], w[N];
+    for (int i = 0; i < N; ++i) { x[i] = xs[i]; w[i] = ws[i]; }
+    const int res = apply_fixup<N, R>(kind, xmin, w, balance, x);
+    if (res == -2) atomicOr(status, kErrFixup);
+    if (res) atomicAdd(counts + (res > 0 ? 0 : 1), 1ull);
+    for (int i = 0; i < N; ++i) xs[i] = x[i];
 }
 
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
@@ -541,7 +562,7 @@ __host__ __device__ constexpr int team_size(int n) {
     return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : n <= 8 ? 8 : n <= 16 ? 16 : 32;
 }
 
-template <int D, int P, typename R, bool PIVOT>
+template <int D, int P, typename R, bool PIVOT, bool FIX = false>
 __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* __restrict__ nodes, int count) {
     constexpr int N1 = P + 1;
     constexpr int N = ipow(N1, D);
@@ -644,6 +665,23 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
         }
     });
 
+    // fixup inputs, before the elimination overwrites A and b: lane r keeps the
+    // column sum w_r = sum_j A[j][r]; bal = sum of the right-hand side
+    R wcol = R(0), bal = R(0);
+    if constexpr (FIX) {
+        static_for<0, N>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            R v = act ? Ar[i] : R(0);
+#pragma unroll
+            for (int off = T / 2; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off, T);
+            if (r == i) wcol = v;
+        });
+        R v = act ? br : R(0);
+#pragma unroll
+        for (int off = T / 2; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off, T);
+        bal = v;
+    }
+
     bool ok = true;
     static_for<0, N>([&](auto kc) {
         constexpr int k = decltype(kc)::value;
@@ -683,6 +721,18 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
         if (r < k) br = fma_r(-Ar[k], xk, br);
     });
     if (!ok && r == 0) atomicOr(s.status, kErrSingular);
+    if constexpr (FIX) {
+        // the team's solution and column sums through shared memory to its
+        // first lane, which applies the fixup as the thread-per-node kernel does
+        __shared__ R fx[256], fw[256];
+        const int base = threadIdx.x - r;
+        fx[threadIdx.x] = br;
+        fw[threadIdx.x] = wcol;
+        __syncwarp(mask);
+        if (r == 0) apply_fixup_mem<N, R>(s.fix_kind, s.fix_min, fx + base, fw + base, bal, s.status, s.fix_counts);
+        __syncwarp(mask);
+        br = fx[threadIdx.x];
+    }
     if (act) s.psi[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)] = br;
 }
 
@@ -691,7 +741,7 @@ __global__ void __launch_bounds__(256) k_sweep_team(SweepArgs<R> s, const int* _
 // thread, and is solved by Gaussian elimination with the team kernel's pivot
 // rule (largest magnitude, first row on ties) and arithmetic (reciprocal of the
 // pivot, multiplier A[i][k] * inv, back substitution by x_k = b_k * inv_k).
-template <int D, int P, typename R, bool PIVOT>
+template <int D, int P, typename R, bool PIVOT, bool FIX = false>
 __global__ void __launch_bounds__(64) k_sweep_block(SweepArgs<R> s, const int* __restrict__ nodes) {
     constexpr int N1 = P + 1;
     constexpr int N = ipow(N1, D);
@@ -777,6 +827,20 @@ __global__ void __launch_bounds__(64) k_sweep_block(SweepArgs<R> s, const int* _
     });
     b[r] = br;
     __syncthreads();
+    // fixup inputs before the elimination: column sums of A, the source total
+    __shared__ R wsh[N];
+    __shared__ R balsh;
+    if constexpr (FIX) {
+        R c = R(0);
+        for (int j = 0; j < N; ++j) c += A[j * LD + r];
+        wsh[r] = c;
+        if (r == 0) {
+            R t = R(0);
+            for (int j = 0; j < N; ++j) t += b[j];
+            balsh = t;
+        }
+        __syncthreads();
+    }
 
     bool ok = true;
     R myinv = R(0);
@@ -830,6 +894,10 @@ __global__ void __launch_bounds__(64) k_sweep_block(SweepArgs<R> s, const int* _
     }
     __syncthreads();
     if (!ok && r == 0) atomicOr(s.status, kErrSingular);
+    if constexpr (FIX) {
+        if (r == 0) apply_fixup_mem<N, R>(s.fix_kind, s.fix_min, b, wsh, balsh, s.status, s.fix_counts);
+        __syncthreads();
+    }
     s.psi[psi_index(s.ndof, s.Nw, g, a, (long long)e * N + r)] = b[r];
 }
 

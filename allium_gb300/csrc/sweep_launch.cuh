@@ -33,7 +33,10 @@ cudaError_t sweep_levels_team(Handle& h, const SweepArgs<R>& args, cudaStream_t 
         const long long threads = (long long)count * h.G * T;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
         const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_team<D, P, R, PIVOT><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count);
+        if (args.fix_kind)
+            k_sweep_team<D, P, R, PIVOT, true><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count);
+        else
+            k_sweep_team<D, P, R, PIVOT, false><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count);
     }
     return cudaGetLastError();
 }
@@ -46,7 +49,10 @@ cudaError_t sweep_levels_block(Handle& h, const SweepArgs<R>& args, cudaStream_t
         if (count == 0) continue;
         const long long blocks = (long long)count * h.G;
         if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
-        k_sweep_block<D, P, R, PIVOT><<<(unsigned)blocks, 64, 0, stream>>>(args, h.d_level_nodes + off);
+        if (args.fix_kind)
+            k_sweep_block<D, P, R, PIVOT, true><<<(unsigned)blocks, 64, 0, stream>>>(args, h.d_level_nodes + off);
+        else
+            k_sweep_block<D, P, R, PIVOT, false><<<(unsigned)blocks, 64, 0, stream>>>(args, h.d_level_nodes + off);
     }
     return cudaGetLastError();
 }

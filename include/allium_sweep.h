@@ -190,7 +190,7 @@ int allium_sweep_set_pipeline(allium_sweep* s, int chunks, int streams, int tape
  * (src/fixup.cpp:59-88; the bound-constrained projection solved exactly instead of
  * by mfem::SLBQPOptimizer's iteration), with the operator's minimum_solution.
  * Where the reference aborts (Ryosuke with more than three positive entries) the
- * sweep returns ALLIUM_ERR_UNSUPPORTED; systems above 8 x 8 are refused.
+ * sweep returns ALLIUM_ERR_UNSUPPORTED.  Every order is supported.
  * While a fixup is on, Mult rebuilds and factors every local system. */
 int allium_sweep_set_fixup(allium_sweep* s, int kind, double minimum);
 

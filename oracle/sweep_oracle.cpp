@@ -588,10 +588,10 @@ int fixup_local_opt(int n, const double* w, double total, double* x, double xmin
     double lam = 0.0;
     bool feasible = false;
     for (int pass = 0; pass <= n; ++pass) {
-        double rest = total, ww = 0.0;
+        double rest = total, ww = 0.0;   // free: w (x0 + lam w); clamped: w * floor; w = 0: nothing
         for (int i = 0; i < n; ++i) {
             if (freev[i]) { rest -= w[i] * x[i]; ww += w[i] * w[i]; }
-            else rest -= w[i] * (x[i] > xmin ? x[i] : xmin);
+            else if (w[i] > 0.0) rest -= w[i] * xmin;
         }
         if (!(ww > 0.0)) break;
         lam = rest / ww;
@@ -600,11 +600,15 @@ int fixup_local_opt(int n, const double* w, double total, double* x, double xmin
             if (freev[i] && x[i] + lam * w[i] < xmin) { freev[i] = 0; clamped = true; }
         if (!clamped) { feasible = true; break; }
     }
+    if (!feasible) {
+        for (int i = 0; i < n; ++i) x[i] = x[i] > xmin ? x[i] : xmin;
+        return -1;
+    }
     for (int i = 0; i < n; ++i) {
-        const double v = freev[i] && feasible ? x[i] + lam * w[i] : x[i];
+        const double v = freev[i] ? x[i] + lam * w[i] : (w[i] > 0.0 ? xmin : x[i]);
         x[i] = v > xmin ? v : xmin;
     }
-    return feasible ? 1 : -1;
+    return 1;
 }
 
 bool linear_solve(int m, double* A /*column major*/, double* x) {

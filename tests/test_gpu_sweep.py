@@ -377,6 +377,42 @@ def test_fixup_parity(dim, cells, kind):
     assert np.array_equal(psi, plain)
 
 
+@pytest.mark.parametrize("dim,cells,p", [(2, (10, 10), 2), (2, (8, 8), 3), (3, (4, 4, 4), 2), (3, (3, 3, 3), 3)])
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
+def test_fixup_high_order(dim, cells, p, kind):
+    # the fixups on the lane-per-row (9..27 DOFs) and block-per-node (64 DOFs)
+    # kernels: one lane of the team applies them to the staged solution
+    mesh = M.cartesian(cells, jitter=0.1, seed=2)
+    quad = Q.level_symmetric(4, dim)
+    sig = np.full((1, mesh.num_elements), 50.0)
+    q = np.zeros((1, mesh.num_elements))
+    q[:, 0] = 100.0
+    o = OracleSweep(mesh, p, quad, sig)
+    L = InverseAdvectionOperator(mesh, p, quad, sig)
+    src = FormTransportSource(L, q)
+    plain = np.empty_like(src)
+    L.Mult(src, plain)
+    assert plain.min() < 0
+    o.set_fixup(kind, 0.0)
+    L.SetFixup(kind, 0.0)
+    ref = o.mult(src)
+    psi = np.empty_like(src)
+    if o.fixup_unsupported():
+        with pytest.raises(AlliumError) as e:
+            L.Mult(src, psi)
+        assert e.value.status == 7
+    else:
+        L.Mult(src, psi)
+        assert psi.min() >= 0.0
+        assert rel_err(psi, ref) < 1e-10
+        applied, failed = L.FixupCounts(reset=True)
+        ra, rf = o.fixup_counts()
+        assert abs(applied - ra) <= max(3, ra // 100) and abs(failed - rf) <= max(3, rf // 100)
+    L.SetFixup(0)
+    L.Mult(src, psi)
+    assert np.array_equal(psi, plain)
+
+
 def test_errors_are_reported():
     mesh, quad, sig = problem(2, (4, 4), 1)
     m3, q3, s3 = problem(3, (2, 2, 2), 3)

@@ -288,3 +288,39 @@ def test_layout_maps():
     assert np.array_equal(relayout(left, G, Nw, nd, to_left=False), right)
     # the LEFT vector is the RIGHT one viewed as [G][Nw][Ndof] and transposed
     assert np.array_equal(left, right.reshape(G, Nw, nd).transpose(2, 1, 0).ravel())
+
+
+@pytest.mark.parametrize("kind", [2, 3, 4])
+def test_oracle_conservative_fixups(kind):
+    # src/fixup.cpp: zero-and-scale (2), Ryosuke (3) and local optimization (4)
+    # make psi >= 0 and keep every cell's balance w . x = sum b, so the global
+    # balance of the sweep (absorption + leakage) equals the unfixed one
+    mesh = M.cartesian((16, 16), jitter=0.1, seed=2)
+    quad = Q.level_symmetric(4, 2)
+    sig = np.full((1, mesh.num_elements), 50.0)
+    q = np.zeros((1, mesh.num_elements))
+    q[:, 0] = 100.0
+    o = OracleSweep(mesh, 1, quad, sig)
+    src = o.form_source(q_cell=q)
+    plain = o.mult(src)
+    assert plain.min() < 0
+    o.set_fixup(kind, 0.0)
+    psi = o.mult(src)
+    applied, failed = o.fixup_counts()
+    assert applied > 0 and failed == 0 and o.fixup_unsupported() == 0
+    assert psi.min() >= 0.0
+    assert abs(o.balance(psi) - o.balance(plain)) < 1e-12 * abs(o.balance(plain))
+
+
+def test_oracle_ryosuke_abort_case():
+    # 3D p = 1: cells with more than three positive entries after the zeroing,
+    # where RyosukeFixupOperator::perform_nff aborts (src/fixup.cpp:155)
+    mesh = M.cartesian((6, 6, 6), jitter=0.1, seed=2)
+    quad = Q.level_symmetric(4, 3)
+    sig = np.full((1, mesh.num_elements), 50.0)
+    q = np.zeros((1, mesh.num_elements))
+    q[:, 0] = 100.0
+    o = OracleSweep(mesh, 1, quad, sig)
+    o.set_fixup(3, 0.0)
+    o.mult(o.form_source(q_cell=q))
+    assert o.fixup_unsupported() > 0
