@@ -168,6 +168,52 @@ def cpu_sweep_sample(threads, steps, warmup, ndir=8):
     return rates, o.psi_size
 
 
+def cpu_trt_sweep_rate(groups=2, steps=3):
+    """CPU oracle sweep rate (DOF*angle*group/s, all cores) on the TRT wave's
+    mesh and quadrature (128 x 128, p = 1, S8) with `groups` of its 32 groups:
+    the cost per group is the same, so the rate carries over."""
+    from oracle.oracle import OracleSweep
+    from allium_gb300 import mesh as M
+    from allium_gb300 import quadrature as Q
+    mesh = M.cartesian((128, 128))
+    quad = Q.level_symmetric(8, 2)
+    sig = np.ones((groups, mesh.num_elements))
+    o = OracleSweep(mesh, 1, quad, sig)
+    src = np.random.default_rng(SEED).random(o.psi_size)
+    psi = np.empty_like(src)
+    o.mult(src, psi, threads=os.cpu_count() or 1)
+    rates = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.mult(src, psi, threads=os.cpu_count() or 1)
+        rates.append(o.psi_size / (time.perf_counter() - t0))
+    return statistics.median(rates)
+
+
+def cpu_extrapolated(line, rate3d, n3d):
+    """CPU time to tolerance of the solver sections, extrapolated as FP64
+    sweeps x CPU sweep time (the all-core oracle restatement of Mult_Upwind;
+    Krylov vector work excluded, so a lower bound): the C2 solve on the 3D
+    workload and the 200-step TRT wave, beside the GPU times."""
+    out = {"kind": "extrapolated: FP64 sweeps x measured CPU sweep time (lower bound)",
+           "cores": os.cpu_count()}
+    t = line.get("time_to_tolerance")
+    if t:
+        sweeps = t["fp64_gmres"]["fp64_sweeps"]
+        cpu_s = sweeps * n3d / rate3d
+        out["c2_fp64_gmres"] = {"seconds": cpu_s, "fp64_sweeps": sweeps, "cpu_sweep_rate": rate3d,
+                                "gpu_seconds": t["fp64_gmres"]["seconds"],
+                                "gpu_speedup": cpu_s / t["fp64_gmres"]["seconds"]}
+    tr = line.get("trt_marshak")
+    if tr:
+        rate2d = cpu_trt_sweep_rate()
+        sweeps = tr["fp64"]["fp64_sweeps"]
+        cpu_s = sweeps * tr["psi_entries"] / rate2d
+        out["c4_trt_fp64"] = {"seconds": cpu_s, "fp64_sweeps": sweeps, "cpu_sweep_rate": rate2d,
+                              "gpu_seconds": tr["fp64"]["seconds"], "gpu_speedup": cpu_s / tr["fp64"]["seconds"]}
+    return out
+
+
 def solve_section(L, mesh, quad, sigma, src, maxiter=400):
     """Time to a 1e-8 relative residual of T phi = b on the 3D workload with
     sigma_s / sigma_t ~ U[0.5, 0.999] per cell: FP64 GMRES(30) with the FP64
@@ -662,6 +708,10 @@ def run_gpu(args):
         rates1, size1 = cpu_sweep_sample(1, 3, 1, ndir=1)
         line["cpu_baseline_1thread"] = {"value": statistics.median(rates1), "unit": UNIT, "cores": 1, "kind": "port",
                                         "sample": f"full 64^3 mesh, 1 of 168 S12 directions, {size1} DOF*angle per sweep, median of 3"}
+        try:
+            line["cpu_time_to_tolerance"] = cpu_extrapolated(line, statistics.median(rates), N)
+        except Exception as exc:   # a reported estimate, never a reason to lose the line
+            line["cpu_time_to_tolerance"] = {"error": repr(exc)}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
