@@ -59,6 +59,8 @@ EXPORTS = {
     "allium_sweep_moments": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "allium_sweep_moments_transpose": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "allium_sweep_form_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "allium_sweep_form_source_general": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "allium_sweep_source_points": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_scattering_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_moments_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_scattering_source_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -609,14 +609,16 @@ int allium_sweep_moments_f32_nodes(allium_sweep* s, const float* psi, double* ph
     return ALLIUM_OK;
 }
 
-int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow, int num_attr, double* source) {
-    if (!s || !source || (inflow && num_attr < 1)) return ALLIUM_ERR_ARG;
-    Handle& h = s->h;
-    double *dq = nullptr, *di = nullptr;
+static int form_source(Handle& h, const double* q_cell, const double* q_points, int q_dir, const double* inflow,
+                       int num_attr, int angular, double* source) {
+    if (!source || (inflow && num_attr < 1)) return ALLIUM_ERR_ARG;
+    const long long np = allium::source_points_per_cell(h);
+    double *dq = nullptr, *dp = nullptr, *di = nullptr;
     int st = ALLIUM_OK;
     if (q_cell) st = upload(h, q_cell, (size_t)h.G * h.ne, &dq);
-    if (!st && inflow) st = upload(h, inflow, (size_t)h.G * num_attr, &di);
-    if (st) { if (dq) cudaFree(dq); if (di) cudaFree(di); return st; }
+    if (!st && q_points) st = upload(h, q_points, (size_t)h.G * (q_dir ? h.Nw : 1) * h.ne * np, &dp);
+    if (!st && inflow) st = upload(h, inflow, (size_t)h.G * (angular ? h.Nw : 1) * num_attr, &di);
+    if (st) { if (dq) cudaFree(dq); if (dp) cudaFree(dp); if (di) cudaFree(di); return st; }
     const bool dsrc = on_device(source);
     double* out = source;
     cudaError_t e = cudaSuccess;
@@ -624,12 +626,42 @@ int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double
         e = ensure(&h.d_stage, (size_t)h.psi_size);
         out = h.d_stage;
     }
-    if (e == cudaSuccess) e = allium::launch_form_source(h, dq, di, inflow ? num_attr : 0, out);
+    if (e == cudaSuccess) e = allium::launch_form_source(h, dq, dp, q_dir, di, inflow ? num_attr : 0, angular, out);
     if (e == cudaSuccess && !dsrc)
         e = cudaMemcpyAsync(source, out, (size_t)h.psi_size * sizeof(double), cudaMemcpyDeviceToHost, h.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
     if (dq) cudaFree(dq);
+    if (dp) cudaFree(dp);
     if (di) cudaFree(di);
+    CUDA_OR_FAIL(h, e);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow, int num_attr, double* source) {
+    if (!s) return ALLIUM_ERR_ARG;
+    return form_source(s->h, q_cell, nullptr, 0, inflow, num_attr, 0, source);
+}
+
+int allium_sweep_form_source_general(allium_sweep* s, const double* q_points, int q_per_direction,
+                                     const double* inflow_angular, int num_attr, double* source) {
+    if (!s || (q_per_direction != 0 && q_per_direction != 1)) return ALLIUM_ERR_ARG;
+    return form_source(s->h, nullptr, q_points, q_per_direction, inflow_angular, num_attr, 1, source);
+}
+
+int allium_sweep_source_points(allium_sweep* s, int* points_per_cell, double* coords) {
+    if (!s || !points_per_cell) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    const long long np = allium::source_points_per_cell(h);
+    *points_per_cell = (int)np;
+    if (!coords) return ALLIUM_OK;
+    const size_t n = (size_t)h.ne * np * h.dim;
+    const bool dc = on_device(coords);
+    double* out = coords;
+    if (!dc) CUDA_OR_FAIL(h, cudaMalloc(&out, n * sizeof(double)));
+    cudaError_t e = allium::launch_source_points(h, out);
+    if (e == cudaSuccess && !dc) e = cudaMemcpyAsync(coords, out, n * sizeof(double), cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    if (!dc) cudaFree(out);
     CUDA_OR_FAIL(h, e);
     return ALLIUM_OK;
 }

@@ -247,7 +247,10 @@ cudaError_t launch_dsa_assemble(Handle& h, const double* sigma_s, double kappa, 
 cudaError_t launch_dsa_apply(Handle& h, const double* x, double* y);
 cudaError_t launch_time_mass(Handle& h);
 int compute_levels(Handle& h);   // returns an allium status
-cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out);
+cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* q_points, int q_dir, const double* inflow,
+                               int nattr, int angular, double* out);
+int source_points_per_cell(const Handle& h);
+cudaError_t launch_source_points(Handle& h, double* out);
 cudaError_t launch_moments(Handle& h, const double* psi, double* phi, int nmom);
 cudaError_t launch_moments_transpose(Handle& h, const double* phi, double* psi, int nmom, double alpha, int add);
 cudaError_t launch_balance(Handle& h, const double* psi, double* partial, int nblocks_max, int* nblocks);

@@ -671,13 +671,45 @@ int build_chunks(Handle& h, int nchunk, int taper) {
 //            + sum_{bdr faces} sum_q w_q (|Omega.n_q| - Omega.n_q)/2 psi_in phi_i
 // with n_q the unnormalised normal (CalcOrtho) at each face point
 // (BoundaryFlowIntegrator with alpha = -1, beta = -1/2).
+// qpts (optional, replaces qcell): the density at the domain rule's points,
+// [G][Ne][points], or [G][Nw][Ne][points] with q_dir, for a coefficient that
+// varies inside a cell (and with the direction): the integral
+// DomainLFIntegrator forms from a FunctionCoefficient.  angular: inflow is
+// [G][Nw][nattr] (a direction-dependent inflow per attribute) instead of
+// [G][nattr].
+__device__ void source_domain_term(const RefTables& t, const double* X, double Q, const double* Qp, double* acc) {
+    const int dim = t.dim, n = t.n, n1 = t.n1, m4 = t.rn[4];
+    int np = 1;
+    for (int d = 0; d < dim; ++d) np *= m4;
+    for (int i = 0; i < n; ++i) acc[i] = 0.0;
+    if (!Qp && Q == 0.0) return;
+    for (int q = 0; q < np; ++q) {
+        int id[3], rq = q;
+        double xi[3], w = 1.0;
+        for (int d = 0; d < dim; ++d) { id[d] = rq % m4; rq /= m4; xi[d] = t.rx[4][id[d]]; w *= t.rw[4][id[d]]; }
+        double J[3][3], A[3][3];
+        cell_jacobian(dim, X, xi, J, nullptr);
+        const double val = adjugate(dim, J, A) * (Qp ? Qp[q] : Q);
+        double v[3][kMaxOrder + 1];
+        for (int d = 0; d < dim; ++d) lagrange1d(n1, t.nodes, xi[d], v[d], nullptr);
+        for (int i = 0; i < n; ++i) {
+            int ii[3]; dof_index(dim, n1, i, ii);
+            double ph = 1.0;
+            for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
+            acc[i] += w * val * ph;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw, int G, long long ndof,
                                                      const double* __restrict__ corners, const double* __restrict__ omega,
                                                      const Slot* __restrict__ slots, const double* __restrict__ qcell,
-                                                     const double* __restrict__ inflow, int nattr, double* __restrict__ out) {
-    // one thread per (g, e): the domain term does not depend on the angle, so
-    // it is integrated once and each angle adds its own boundary terms to a
-    // copy (the same sums in the same order as integrating per angle)
+                                                     const double* __restrict__ qpts, int q_dir,
+                                                     const double* __restrict__ inflow, int nattr, int angular,
+                                                     double* __restrict__ out) {
+    // one thread per (g, e): a direction-independent domain term is
+    // integrated once and each angle adds its own boundary terms to a copy
+    // (the same sums in the same order as integrating per angle)
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= (long long)G * ne) return;
     const int e = (int)(tid % ne);
@@ -685,74 +717,55 @@ __global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw
     const int dim = t.dim, n = t.n, n1 = t.n1, nc = 1 << dim;
     double X[24];
     for (int q = 0; q < nc * dim; ++q) X[q] = corners[(size_t)e * nc * dim + q];
-    double vol[64];
-    for (int i = 0; i < n; ++i) vol[i] = 0.0;
-    const double Q = qcell ? qcell[(size_t)g * ne + e] : 0.0;
-    const int m4 = t.rn[4];
     int np = 1;
-    for (int d = 0; d < dim; ++d) np *= m4;
-    if (Q != 0.0) {
-        for (int q = 0; q < np; ++q) {
-            int id[3], rq = q;
-            double xi[3], w = 1.0;
-            for (int d = 0; d < dim; ++d) { id[d] = rq % m4; rq /= m4; xi[d] = t.rx[4][id[d]]; w *= t.rw[4][id[d]]; }
-            double J[3][3], A[3][3];
-            cell_jacobian(dim, X, xi, J, nullptr);
-            const double val = adjugate(dim, J, A) * Q;
-            double v[3][kMaxOrder + 1];
-            for (int d = 0; d < dim; ++d) lagrange1d(n1, t.nodes, xi[d], v[d], nullptr);
-            for (int i = 0; i < n; ++i) {
-                int ii[3]; dof_index(dim, n1, i, ii);
-                double ph = 1.0;
-                for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
-                vol[i] += w * val * ph;
-            }
-        }
-    }
-    // boundary faces of this cell that carry a non-zero inflow
+    for (int d = 0; d < dim; ++d) np *= t.rn[4];
+    const double Q = qcell ? qcell[(size_t)g * ne + e] : 0.0;
+    double vol[64];
+    if (!(qpts && q_dir)) source_domain_term(t, X, Q, qpts ? qpts + ((size_t)g * ne + e) * np : nullptr, vol);
+    // boundary faces of this cell that may carry inflow
     bool any_inflow = false;
     if (inflow)
         for (int k = 0; k < 2 * dim; ++k) {
             const Slot s = slots[(size_t)e * 2 * dim + k];
-            if (s.nbr < 0 && s.attr >= 0 && s.attr < nattr && inflow[(size_t)g * nattr + s.attr] != 0.0) any_inflow = true;
+            if (s.nbr < 0 && s.attr >= 0 && s.attr < nattr && (angular || inflow[(size_t)g * nattr + s.attr] != 0.0))
+                any_inflow = true;
         }
     const int m5 = t.rn[5];
     int npf = 1;
     for (int d = 0; d < dim - 1; ++d) npf *= m5;
     for (int a = 0; a < Nw; ++a) {
         double* o = out + psi_index(ndof, Nw, g, a, (long long)e * n);
-        if (!any_inflow) {
-            for (int i = 0; i < n; ++i) o[i] = vol[i];
-            continue;
-        }
         double acc[64];
-        for (int i = 0; i < n; ++i) acc[i] = vol[i];
-        double om[3] = {0, 0, 0};
-        for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
-        for (int k = 0; k < 2 * dim; ++k) {
-            const Slot s = slots[(size_t)e * 2 * dim + k];
-            if (s.nbr >= 0 || s.attr < 0 || s.attr >= nattr) continue;
-            const double fin = inflow[(size_t)g * nattr + s.attr];
-            if (fin == 0.0) continue;
-            for (int q = 0; q < npf; ++q) {
-                int id[3], rq = q;
-                double tt[2] = {0, 0}, w = 1.0;
-                for (int d = 0; d < dim - 1; ++d) { id[d] = rq % m5; rq /= m5; tt[d] = t.rx[5][id[d]]; w *= t.rw[5][id[d]]; }
-                double xi[3], J[3][3], A[3][3];
-                face_to_cell(dim, k, tt, xi);
-                cell_jacobian(dim, X, xi, J, nullptr);
-                adjugate(dim, J, A);
-                const double sg = (k % 2) ? 1.0 : -1.0;
-                double un = 0.0;
-                for (int d = 0; d < dim; ++d) un += om[d] * (sg * A[k / 2][d]);
-                const double wt = (0.5 * -1.0 * un - (-0.5) * fabs(un)) * (w * fin);
-                double v[3][kMaxOrder + 1];
-                for (int d = 0; d < dim; ++d) lagrange1d(n1, t.nodes, xi[d], v[d], nullptr);
-                for (int i = 0; i < n; ++i) {
-                    int ii[3]; dof_index(dim, n1, i, ii);
-                    double ph = 1.0;
-                    for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
-                    acc[i] += wt * ph;
+        if (qpts && q_dir) source_domain_term(t, X, 0.0, qpts + (((size_t)g * Nw + a) * ne + e) * np, acc);
+        else for (int i = 0; i < n; ++i) acc[i] = vol[i];
+        if (any_inflow) {
+            double om[3] = {0, 0, 0};
+            for (int d = 0; d < dim; ++d) om[d] = omega[a * dim + d];
+            for (int k = 0; k < 2 * dim; ++k) {
+                const Slot s = slots[(size_t)e * 2 * dim + k];
+                if (s.nbr >= 0 || s.attr < 0 || s.attr >= nattr) continue;
+                const double fin = angular ? inflow[((size_t)g * Nw + a) * nattr + s.attr] : inflow[(size_t)g * nattr + s.attr];
+                if (fin == 0.0) continue;
+                for (int q = 0; q < npf; ++q) {
+                    int id[3], rq = q;
+                    double tt[2] = {0, 0}, w = 1.0;
+                    for (int d = 0; d < dim - 1; ++d) { id[d] = rq % m5; rq /= m5; tt[d] = t.rx[5][id[d]]; w *= t.rw[5][id[d]]; }
+                    double xi[3], J[3][3], A[3][3];
+                    face_to_cell(dim, k, tt, xi);
+                    cell_jacobian(dim, X, xi, J, nullptr);
+                    adjugate(dim, J, A);
+                    const double sg = (k % 2) ? 1.0 : -1.0;
+                    double un = 0.0;
+                    for (int d = 0; d < dim; ++d) un += om[d] * (sg * A[k / 2][d]);
+                    const double wt = (0.5 * -1.0 * un - (-0.5) * fabs(un)) * (w * fin);
+                    double v[3][kMaxOrder + 1];
+                    for (int d = 0; d < dim; ++d) lagrange1d(n1, t.nodes, xi[d], v[d], nullptr);
+                    for (int i = 0; i < n; ++i) {
+                        int ii[3]; dof_index(dim, n1, i, ii);
+                        double ph = 1.0;
+                        for (int d = 0; d < dim; ++d) ph *= v[d][ii[d]];
+                        acc[i] += wt * ph;
+                    }
                 }
             }
         }
@@ -760,11 +773,43 @@ __global__ void __launch_bounds__(128) k_form_source(RefTables t, int ne, int Nw
     }
 }
 
-cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* inflow, int nattr, double* out) {
+cudaError_t launch_form_source(Handle& h, const double* q_cell, const double* q_points, int q_dir, const double* inflow,
+                               int nattr, int angular, double* out) {
     const long long total = (long long)h.G * h.ne;
     const int b = 128;
     k_form_source<<<(unsigned)((total + b - 1) / b), b, 0, h.stream>>>(h.ref, h.ne, h.Nw, h.G, h.ndof, h.d_corners, h.d_omega,
-                                                                       h.d_slots, q_cell, inflow, nattr, out);
+                                                                       h.d_slots, q_cell, q_points, q_dir, inflow, nattr,
+                                                                       angular, out);
+    return cudaGetLastError();
+}
+
+// Physical coordinates of the source rule's points, [Ne][points][dim], in the
+// order k_form_source takes their densities.
+__global__ void k_source_points(RefTables t, int ne, const double* __restrict__ corners, double* __restrict__ out) {
+    const int dim = t.dim, nc = 1 << dim, m4 = t.rn[4];
+    int np = 1;
+    for (int d = 0; d < dim; ++d) np *= m4;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)ne * np) return;
+    const int e = (int)(tid / np), q = (int)(tid % np);
+    double X[24];
+    for (int c = 0; c < nc * dim; ++c) X[c] = corners[(size_t)e * nc * dim + c];
+    int rq = q;
+    double xi[3] = {0, 0, 0}, J[3][3], x[3];
+    for (int d = 0; d < dim; ++d) { xi[d] = t.rx[4][rq % m4]; rq /= m4; }
+    cell_jacobian(dim, X, xi, J, x);
+    for (int d = 0; d < dim; ++d) out[tid * dim + d] = x[d];
+}
+
+int source_points_per_cell(const Handle& h) {
+    int np = 1;
+    for (int d = 0; d < h.dim; ++d) np *= h.ref.rn[4];
+    return np;
+}
+
+cudaError_t launch_source_points(Handle& h, double* out) {
+    const long long total = (long long)h.ne * source_points_per_cell(h);
+    k_source_points<<<(unsigned)((total + 127) / 128), 128, 0, h.stream>>>(h.ref, h.ne, h.d_corners, out);
     return cudaGetLastError();
 }
 

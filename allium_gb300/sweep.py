@@ -352,6 +352,48 @@ def FormTransportSource(Linv: InverseAdvectionOperator, q_cell=None, inflow=None
     return out
 
 
+def SourcePoints(Linv: InverseAdvectionOperator):
+    """Physical coordinates [Ne, P, dim] of the source's domain-rule points."""
+    L = _lib.lib()
+    npc = C.c_int()
+    check(L.allium_sweep_source_points(Linv.h, C.byref(npc), None), Linv.h)
+    out = np.empty((Linv.mesh.num_elements, npc.value, Linv.dim))
+    check(L.allium_sweep_source_points(Linv.h, C.byref(npc), C.c_void_p(out.ctypes.data)), Linv.h)
+    return out
+
+
+def FormTransportSourceGeneral(Linv: InverseAdvectionOperator, q_fn=None, inflow_angular=None, out=None,
+                               per_direction=False):
+    """Weak-form source for a density evaluated at the domain-rule points:
+    q_fn(x, g) -> [Ne, P] (x: [Ne, P, dim] coordinates), or with per_direction
+    q_fn(x, omega, g) -> [Ne, P] for each direction omega; and a
+    direction-dependent inflow_angular[G, Nw, num_attr] per boundary attribute."""
+    L = _lib.lib()
+    if out is None:
+        out = np.empty(Linv.width)
+    qp = inp = None
+    nattr = 0
+    keep = []
+    if q_fn is not None:
+        x = SourcePoints(Linv)
+        shape = x.shape[:2]
+        if per_direction:
+            q = np.stack([np.stack([np.asarray(q_fn(x, Linv.quad.omega[a], g), dtype=np.float64).reshape(shape)
+                                    for a in range(Linv.Nw)]) for g in range(Linv.G)])
+        else:
+            q = np.stack([np.asarray(q_fn(x, g), dtype=np.float64).reshape(shape) for g in range(Linv.G)])
+        q = np.ascontiguousarray(q)
+        keep.append(q)
+        qp = q.ctypes.data
+    if inflow_angular is not None:
+        fin = np.ascontiguousarray(inflow_angular, dtype=np.float64).reshape(Linv.G, Linv.Nw, -1)
+        keep.append(fin)
+        inp, nattr = fin.ctypes.data, fin.shape[2]
+    check(L.allium_sweep_form_source_general(Linv.h, C.c_void_p(qp), int(bool(per_direction)), C.c_void_p(inp), nattr,
+                                             C.c_void_p(_ptr(out, np.float64, Linv.width, "source"))), Linv.h)
+    return out
+
+
 class TransportOperator:
     """I - D L^{-1} S D^T applied to phi (src/transport_op.hpp:9-35).  S is a
     callable phi -> S phi (the scattering mass), psi the work vector."""

@@ -241,6 +241,24 @@ int allium_sweep_moments_transpose(allium_sweep* s, const double* phi, double* p
 int allium_sweep_form_source(allium_sweep* s, const double* q_cell, const double* inflow,
                              int num_attr, double* source);
 
+/* FormTransportSource for coefficients that vary inside a cell and with the
+ * direction (src/sweep.cpp:1135-1185 with a FunctionCoefficient source and a
+ * PhaseSpaceCoefficient inflow constant along each boundary attribute):
+ * q_points the density at the P domain-rule points of every cell (their
+ * coordinates from allium_sweep_source_points; NULL for none), [G][Ne][P], or
+ * [G][Nw][Ne][P] per direction when q_per_direction is 1 (a PhaseSpaceCoefficient
+ * source such as the manufactured solutions' of test/test_transport_mms.cpp);
+ * inflow_angular [G][Nw][num_attr] the inflow psi of each direction per
+ * boundary attribute (NULL for vacuum).  Integrated with the same rules as
+ * allium_sweep_form_source, which it equals for constant data. */
+int allium_sweep_form_source_general(allium_sweep* s, const double* q_points, int q_per_direction,
+                                     const double* inflow_angular, int num_attr, double* source);
+
+/* Points of the source's domain rule (DomainLFIntegrator, order 2p: p + 1
+ * Gauss-Legendre points per axis): *points_per_cell = P and, when coords is
+ * not NULL, their physical coordinates [Ne][P][dim] (host or device). */
+int allium_sweep_source_points(allium_sweep* s, int* points_per_cell, double* coords);
+
 /* Isotropic scattering source around the sweep: out = D^T (S phi) + q_fixed,
  * S = sigma_s [G][Ne] times the MassIntegrator matrix of each cell (within-group
  * scattering), as chive's source iteration and MomentMethodFixedPointOperator::Mult

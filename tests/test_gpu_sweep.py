@@ -161,6 +161,45 @@ def test_sources(case):
     assert rel_err(ScatteringSource(L, sig_s, phi, qf), o.scattering_source(sig_s, phi, qf)) < 1e-13
 
 
+@pytest.mark.parametrize("case", CASES[1:: 3], ids=[f"d{c[0]}p{c[2]}" for c in CASES[1:: 3]])
+def test_general_source(case):
+    # point densities and direction-dependent inflow: constant data reproduce
+    # allium_sweep_form_source bit for bit; a density varying in x and with the
+    # direction (a PhaseSpaceCoefficient) matches the oracle's integration
+    from allium_gb300.sweep import FormTransportSourceGeneral, SourcePoints
+    mesh, quad, sig, o, L = build(*case)
+    G, dim = sig.shape[0], mesh.dim
+    rng = np.random.default_rng(8)
+    q = rng.random((G, mesh.num_elements))
+    inflow = rng.random((G, 8))
+    x = SourcePoints(L)
+    assert x.shape[0] == mesh.num_elements and x.shape[2] == dim
+    lo, hi = mesh.vertices.min(0), mesh.vertices.max(0)
+    assert np.all(x >= lo - 1e-12) and np.all(x <= hi + 1e-12)
+    ref = FormTransportSource(L, q, inflow)
+    gen = FormTransportSourceGeneral(L, lambda xx, g: np.repeat(q[g][:, None], xx.shape[1], axis=1),
+                                     np.repeat(inflow[:, None, :], quad.size, axis=1))
+    assert np.array_equal(gen, ref)
+
+    def qx(xx, om, g):   # the oracle's callback form, one point at a time
+        return (1.0 + g) * (2.0 + math.sin(3.0 * xx[0]) * (1.0 + 0.5 * om[0]) + (xx[1] if dim > 1 else 0.0) ** 2)
+
+    def qv(xx, om, g):   # the same, vectorised over the rule points
+        y = xx[..., 1] ** 2 if dim > 1 else 0.0
+        return (1.0 + g) * (2.0 + np.sin(3.0 * xx[..., 0]) * (1.0 + 0.5 * om[0]) + y)
+
+    fin = rng.random((G, quad.size, 8))
+    gen = FormTransportSourceGeneral(L, qv, fin, per_direction=True)
+    want = o.form_source(qfn=qx, inflow_fn=lambda xx, om, g, attr: fin[g, _angle(quad, om), attr])
+    assert rel_err(gen, want) < 1e-13
+
+
+def _angle(quad, om):
+    """Index of the quadrature direction om (a ctypes pointer from the oracle)."""
+    v = np.array([om[i] for i in range(quad.dim)])
+    return int(np.argmin(np.abs(quad.omega - v[None, :]).sum(1)))
+
+
 @pytest.mark.parametrize("dim,cells", [(2, (9, 7)), (3, (6, 5, 4))])
 def test_time_absorption(dim, cells):
     mesh, quad, sig, o, L = build(dim, cells, 1, 4, 2, 0.2, 0)
