@@ -280,7 +280,10 @@ int allium_sweep_scattering_source_f32(allium_sweep* s, const double* sigma_s, c
  * layout stores v[((e*Nw + a)*G + g)*n + i]: in a wavefront level the
  * consecutive angles of one cell, and their upwind traces, are contiguous.
  * Conversions to/from allium's RIGHT FP64 layout, the FP32 sweep (in place
- * allowed; local systems in FP32, unpivoted), the scattering source
+ * allowed; local systems in FP32, unpivoted, or the FP32 copy of the stored
+ * inverses; no negative-flux fixup: it is the linear inner operator of an
+ * FP64 outer iteration, as allium switches the fixup off around its linear
+ * solves, src/trt_linearized.cpp:237-239), the scattering source
  * D^T (S phi) + q (S phi in FP64) and the FP64-accumulated zeroth moment. */
 int allium_sweep_to_node_layout_f32(allium_sweep* s, const double* psi_right, float* out_nodes);
 int allium_sweep_from_node_layout_f32(allium_sweep* s, const float* in_nodes, double* psi_right);
