@@ -1,7 +1,7 @@
-"""The angle-sharded source iteration on two CPU ranks (gloo): each rank
-sweeps half of the directions with the oracle standing in for its GPU, one
-allreduce of the moments per iteration; the result equals the unsharded
-iteration to 1e-10 relative."""
+"""The angle-sharded source iteration on two and three CPU ranks (gloo): each
+rank sweeps its slice of the directions with the oracle standing in for its
+GPU, one allreduce of the moments per iteration; the result equals the
+unsharded iteration to 1e-10 relative."""
 import os
 import socket
 
@@ -49,15 +49,18 @@ def _worker(rank, world, port, path):
     dist.destroy_process_group()
 
 
-def test_angle_sharded_si_two_ranks(tmp_path):
+@pytest.mark.parametrize("world", [2, 3])
+def test_angle_sharded_si(tmp_path, world):
+    # 2 ranks: even halves of the 24 directions; 3 ranks: slices of 8
     mp = pytest.importorskip("torch.multiprocessing")
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
     path = str(tmp_path / "phi")
-    mp.spawn(_worker, args=(2, port, path), nprocs=2, join=True)
-    r0, r1 = np.load(f"{path}.0.npy"), np.load(f"{path}.1.npy")
-    assert np.array_equal(r0, r1)            # every rank holds the same reduced moments
+    mp.spawn(_worker, args=(world, port, path), nprocs=world, join=True)
+    rs = [np.load(f"{path}.{r}.npy") for r in range(world)]
+    r0 = rs[0]
+    assert all(np.array_equal(r0, r) for r in rs[1:])   # every rank holds the same reduced moments
     assert r0[-1] == 1.0
     # the unsharded iteration with the full quadrature
     from oracle.oracle import OracleSweep
