@@ -32,7 +32,9 @@ def test_face_blocks_known_answer(lump):
 
 CONST_CASES = [(1, (10,), 0, 0), (1, (10,), 1, 0), (1, (10,), 1, 7), (1, (10,), 2, 0), (1, (10,), 3, 0),
                (2, (10, 10), 0, 0), (2, (10, 10), 1, 0), (2, (10, 10), 1, 7), (2, (10, 10), 2, 0),
-               (3, (10, 10, 10), 0, 0), (3, (6, 6, 6), 1, 0), (3, (6, 6, 6), 1, 7), (3, (3, 3, 3), 2, 0)]
+               (2, (6, 6), 3, 0),
+               (3, (10, 10, 10), 0, 0), (3, (6, 6, 6), 1, 0), (3, (6, 6, 6), 1, 7), (3, (3, 3, 3), 2, 0),
+               (3, (3, 3, 2), 3, 0)]
 
 
 @pytest.mark.parametrize("dim,cells,p,lump", CONST_CASES)
@@ -46,14 +48,15 @@ def test_constant_solution(dim, cells, p, lump):
     assert np.max(np.abs(psi - 1.0)) < 1e-10
 
 
-@pytest.mark.parametrize("dim,cells,lump", [(1, (10,), 0), (2, (3, 3), 0), (3, (3, 3, 3), 0),
-                                            (1, (10,), 7), (2, (3, 3), 7), (3, (3, 3, 3), 7)])
-def test_L_Linv_identity(dim, cells, lump):
-    # test_sweep.cpp:289-361: || L^{-1} (L x) - x || < 1e-12, sigma = (1, 0.5)
+@pytest.mark.parametrize("dim,cells,lump,p", [(1, (10,), 0, 1), (2, (3, 3), 0, 1), (3, (3, 3, 3), 0, 1),
+                                              (1, (10,), 7, 1), (2, (3, 3), 7, 1), (3, (3, 3, 3), 7, 1),
+                                              (3, (2, 2, 2), 0, 3)])
+def test_L_Linv_identity(dim, cells, lump, p):
+    # test_sweep.cpp:289-361: || L^{-1} (L x) - x || < 1e-12, sigma = (1, 0.5); also 3D p = 3
     mesh = M.cartesian(cells)
     quad = Q.level_symmetric(4, dim)
     sig = np.array([[1.0], [0.5]]) * np.ones((2, mesh.num_elements))
-    o = OracleSweep(mesh, 1, quad, sig, lump=lump)
+    o = OracleSweep(mesh, p, quad, sig, lump=lump)
     x = np.random.default_rng(12345).random(o.psi_size)
     psi = o.mult(o.apply_L(x))
     assert np.linalg.norm(psi - x) < 1e-12
