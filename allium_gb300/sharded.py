@@ -68,18 +68,48 @@ class GPUBackend:
 
 class AngleShardedSI:
     """Source iteration phi <- D L^{-1} (D^T M_s phi + q) with directions
-    split over the ranks of `group` (torch.distributed)."""
+    split over the ranks of `group` (torch.distributed).
 
-    def __init__(self, mesh, order, quad, sigma_t, sigma_s, rank, world, backend=GPUBackend, group=None):
-        self.a0, self.a1 = angle_slice(quad.size, rank, world)
+    group_shards > 1 also splits the groups: the world is a grid of
+    group_shards x (world / group_shards) ranks, rank = ig * na + ia with ia
+    the direction slice and ig the group slice.  Within-group scattering does
+    not couple groups, so the moment allreduce runs only among the na ranks of
+    one group slice; the convergence test sums the squared norms over all
+    ranks.  Every rank must construct the solver (the sub-communicators are
+    created collectively)."""
+
+    def __init__(self, mesh, order, quad, sigma_t, sigma_s, rank, world, backend=GPUBackend, group=None,
+                 group_shards=1):
+        import torch.distributed as dist
+        sigma_t = np.ascontiguousarray(sigma_t, dtype=np.float64)
+        sigma_s = np.ascontiguousarray(sigma_s, dtype=np.float64)
+        G = sigma_t.shape[0]
+        if group_shards < 1 or world % group_shards or group_shards > G:
+            raise ValueError("group_shards must divide the world size and not exceed the group count")
+        na = world // group_shards
+        ia, ig = rank % na, rank // na
+        self.na, self.ng = na, group_shards
+        self.a0, self.a1 = angle_slice(quad.size, ia, na)
+        self.g0, self.g1 = angle_slice(G, ig, group_shards)
         sub = sub_quadrature(quad, self.a0, self.a1)
         scale = float(np.sum(sub.weights) / np.sum(quad.weights))
-        self.sigma_s = np.ascontiguousarray(sigma_s, dtype=np.float64) * scale
-        self.b = backend(mesh, order, sub, sigma_t)
-        self.group = group
+        self.sigma_s = sigma_s[self.g0:self.g1] * scale
+        self.b = backend(mesh, order, sub, np.ascontiguousarray(sigma_t[self.g0:self.g1]))
+        self.world_group = group
+        if group_shards == 1:
+            self.group = group
+        else:
+            # one communicator per group slice, created by every rank in the same order
+            self.group = None
+            for k in range(group_shards):
+                g = dist.new_group(ranks=[k * na + j for j in range(na)])
+                if k == ig:
+                    self.group = g
 
     def solve(self, q_cell, tol=1e-8, maxiter=1000):
+        """Returns (phi of this rank's groups [g1 - g0] x Ndof, iterations, converged)."""
         import torch.distributed as dist
+        q_cell = np.ascontiguousarray(q_cell, dtype=np.float64)[self.g0:self.g1]
         q = self.b.source(q_cell)
         phi = None
         it = 0
@@ -91,7 +121,14 @@ class AngleShardedSI:
             new = self.b.moments(psi)
             dist.all_reduce(new, op=dist.ReduceOp.SUM, group=self.group)   # the one exchange
             it += 1
-            change = (torch.linalg.norm(new - zero) / torch.linalg.norm(new)).item()
+            if self.ng == 1:
+                change = (torch.linalg.norm(new - zero) / torch.linalg.norm(new)).item()
+            else:
+                # every rank of a group slice holds the same moments: the world sums
+                # count each slice na times, which cancels in the ratio
+                sq = torch.stack([torch.sum((new - zero) ** 2), torch.sum(new * new)])
+                dist.all_reduce(sq, op=dist.ReduceOp.SUM, group=self.world_group)
+                change = float(torch.sqrt(sq[0] / sq[1]).item())
             phi = new
             if change < tol:
                 break

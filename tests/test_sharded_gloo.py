@@ -36,17 +36,53 @@ def _case():
     return mesh, quad, sigma, 0.8 * sigma, np.ones((2, mesh.num_elements))
 
 
-def _worker(rank, world, port, path):
+def _worker(rank, world, port, path, group_shards=1):
     import torch.distributed as dist
     from allium_gb300.sharded import AngleShardedSI
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     mesh, quad, sigma, ss, q = _case()
-    solver = AngleShardedSI(mesh, 1, quad, sigma, ss, rank, world, backend=OracleBackend)
+    solver = AngleShardedSI(mesh, 1, quad, sigma, ss, rank, world, backend=OracleBackend, group_shards=group_shards)
     phi, it, conv = solver.solve(q, tol=1e-12, maxiter=500)
-    np.save(f"{path}.{rank}.npy", np.concatenate([phi.numpy(), [it, conv]]))
+    np.save(f"{path}.{rank}.npy", np.concatenate([phi.numpy(), [solver.g0, solver.g1, it, conv]]))
     dist.destroy_process_group()
+
+
+def _unsharded():
+    from oracle.oracle import OracleSweep
+    mesh, quad, sigma, ss, q = _case()
+    o = OracleSweep(mesh, 1, quad, sigma)
+    src = o.form_source(q_cell=q)
+    phi = np.zeros(o.G * o.ndof)
+    for it in range(1, 501):
+        new = o.moments(o.mult(o.scattering_source(ss, phi, src)))
+        done = np.linalg.norm(new - phi) / np.linalg.norm(new) < 1e-12
+        phi = new
+        if done:
+            break
+    return phi.reshape(o.G, -1), it
+
+
+@pytest.mark.parametrize("world,group_shards", [(2, 2), (4, 2)])
+def test_angle_and_group_sharded_si(tmp_path, world, group_shards):
+    # ranks on a (group slice x direction slice) grid: 2 ranks = one group each,
+    # all directions; 4 ranks = 2 group slices x 2 direction slices
+    mp = pytest.importorskip("torch.multiprocessing")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    path = str(tmp_path / "phi")
+    mp.spawn(_worker, args=(world, port, path, group_shards), nprocs=world, join=True)
+    ref, it_ref = _unsharded()
+    na = world // group_shards
+    for r in range(world):
+        res = np.load(f"{path}.{r}.npy")
+        g0, g1, it, conv = int(res[-4]), int(res[-3]), int(res[-2]), res[-1]
+        assert conv == 1.0 and it == it_ref
+        got = res[:-4].reshape(g1 - g0, -1)
+        assert np.max(np.abs(got - ref[g0:g1])) < 1e-10 * np.max(np.abs(ref))
+        assert (g0, g1) == ((r // na), (r // na) + 1)
 
 
 @pytest.mark.parametrize("world", [2, 3])
@@ -62,6 +98,7 @@ def test_angle_sharded_si(tmp_path, world):
     r0 = rs[0]
     assert all(np.array_equal(r0, r) for r in rs[1:])   # every rank holds the same reduced moments
     assert r0[-1] == 1.0
+    r0 = np.concatenate([r0[:-4], r0[-2:]])   # drop the group range (all groups here)
     # the unsharded iteration with the full quadrature
     from oracle.oracle import OracleSweep
     mesh, quad, sigma, ss, q = _case()
