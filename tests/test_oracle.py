@@ -327,3 +327,77 @@ def test_oracle_ryosuke_abort_case():
     o.set_fixup(3, 0.0)
     o.mult(o.form_source(q_cell=q))
     assert o.fixup_unsupported() > 0
+
+
+def _gll(p):
+    if p == 2:
+        return np.array([0.0, 0.5, 1.0])
+    r = 1.0 / math.sqrt(5.0)
+    return np.array([0.0, 0.5 * (1 - r), 0.5 * (1 + r), 1.0])
+
+
+def _lagrange(nodes, t):
+    """Values and derivatives of the Lagrange polynomials on nodes at points t."""
+    n = len(nodes)
+    V = np.ones((n, len(t)))
+    D = np.zeros((n, len(t)))
+    for a in range(n):
+        for b in range(n):
+            if b == a:
+                continue
+            V[a] *= (t - nodes[b]) / (nodes[a] - nodes[b])
+        for c in range(n):
+            if c == a:
+                continue
+            term = np.full(len(t), 1.0 / (nodes[a] - nodes[c]))
+            for b in range(n):
+                if b not in (a, c):
+                    term *= (t - nodes[b]) / (nodes[a] - nodes[b])
+            D[a] += term
+    return V, D
+
+
+@pytest.mark.parametrize("dim,p", [(2, 2), (2, 3), (3, 2)])
+def test_high_order_matrices_on_affine_cells(dim, p):
+    # p >= 2 on affine cells: every integrand is a polynomial that the
+    # integration rules integrate exactly, so the oracle's blocks must equal the
+    # exact integrals, computed here independently by 12-point Gauss-Legendre
+    # on the Lagrange-Gauss-Lobatto basis.  2 x 1 (x 1) cells of the unit square
+    # (cube): 0.5 x 1 (x 1).
+    mesh = M.cartesian((2,) + (1,) * (dim - 1))
+    o = OracleSweep(mesh, p, Q.level_symmetric(4, dim), np.ones((1, 2)))
+    x, w = np.polynomial.legendre.leggauss(12)
+    t, w = 0.5 * (x + 1.0), 0.5 * w
+    V, Dv = _lagrange(_gll(p), t)
+    m1 = (V * w) @ V.T                     # int l_a l_b
+    d1 = (Dv * w) @ V.T                    # d1[a, b] = int l_a' l_b
+    n1 = p + 1
+    h = [0.5] + [1.0] * (dim - 1)
+    vol = float(np.prod(h))
+
+    def kron_axes(mats):
+        # local DOF i = i0 + n1 i1 + n1^2 i2: the last axis varies slowest
+        out = np.ones((1, 1))
+        for m in mats[::-1]:
+            out = np.kron(out, m)
+        return out
+
+    Gm, Mm = o.element_matrices(0)
+    assert np.max(np.abs(Mm - kron_axes([m1] * dim) * vol)) < 1e-14
+    # G_d(i, j) = -int phi_j d_d phi_i = -(vol / h_d) * (int l'_i l_j along d) * masses across
+    for d in range(dim):
+        mats = [d1 if k == d else m1 for k in range(dim)]
+        assert np.max(np.abs(Gm[d] - (-kron_axes(mats) * vol / h[d]))) < 1e-13
+    # interior face x = 1/2 (area 1): blocks on the face DOFs, i0 = p of cell 0, i0 = 0 of cell 1
+    f = [k for k in range(o.num_faces()) if o.face_info(k)[0][2] >= 0][0]
+    F = o.face_matrices(f)
+    tang = kron_axes([m1] * (dim - 1))
+    nf = n1 ** (dim - 1)
+    ex = np.zeros((2, 2, n1 ** dim, n1 ** dim))
+    side = {0: p, 1: 0}
+    for a in (0, 1):
+        for b in (0, 1):
+            for r in range(nf):
+                for c in range(nf):
+                    ex[a, b, side[a] + n1 * r, side[b] + n1 * c] = tang[r, c]
+    assert np.max(np.abs(F - ex)) < 1e-14
