@@ -401,3 +401,35 @@ def test_high_order_matrices_on_affine_cells(dim, p):
                 for c in range(nf):
                     ex[a, b, side[a] + n1 * r, side[b] + n1 * c] = tang[r, c]
     assert np.max(np.abs(F - ex)) < 1e-14
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_transport_source_on_affine_cells(p):
+    # FormTransportSource (src/sweep.cpp:1135-1185) on a 0.5 x 1 affine cell:
+    # q = int Q phi_i = Q vol (int l_ix)(int l_iy), and the inflow term of the
+    # face x = 0 for directions entering through it, |Omega_x| psi_in int_face phi_i
+    mesh = M.cartesian((2, 1))
+    quad = Q.level_symmetric(4, 2)
+    o = OracleSweep(mesh, p, quad, np.ones((1, 2)))
+    x, w = np.polynomial.legendre.leggauss(12)
+    t, w = 0.5 * (x + 1.0), 0.5 * w
+    V, _ = _lagrange(_gll(p), t)
+    s1 = V @ w                              # int l_a
+    n1 = p + 1
+    qv = 1.7
+    src = o.form_source(q_cell=np.full((1, 2), qv)).reshape(quad.size, 2, n1 * n1)
+    exact = qv * 0.5 * np.kron(s1, s1)
+    assert np.max(np.abs(src[:, 0, :] - exact[None, :])) < 1e-14
+    # inflow psi_in = 2 on the left boundary (attribute 4 of the cartesian mesh)
+    attrs = np.unique(mesh.boundary_attributes)
+    left = [a for a in attrs if np.allclose(mesh.vertices[mesh.boundary_faces[mesh.boundary_attributes == a]][..., 0], 0.0)]
+    assert len(left) == 1
+    inflow = np.zeros((1, int(attrs.max()) + 1))
+    inflow[0, left[0]] = 2.0
+    srcb = o.form_source(inflow=inflow).reshape(quad.size, 2, n1 * n1)
+    for a in range(quad.size):
+        ox = quad.omega[a, 0]
+        want = np.zeros(n1 * n1)
+        if ox > 0:   # enters through x = 0: DOFs with ix = 0, weight |Omega_x| * 2 * int l_iy
+            want[0::n1] = ox * 2.0 * s1
+        assert np.max(np.abs(srcb[a, 0] - want)) < 1e-14
