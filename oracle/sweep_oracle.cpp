@@ -835,7 +835,8 @@ void oracle_element_matrices(void* h, int e, int g, double* Gout, double* Mout) 
 }
 
 void oracle_time_mass(void* h, int e, double* Mout) {
-    const Oracle& o = *static_cast<Oracle*>(h);
+    Oracle& o = *static_cast<Oracle*>(h);
+    if (o.Mt.empty()) assemble_time_mass(o);   // assembled on first use
     const size_t nn = (size_t)o.n * o.n;
     std::memcpy(Mout, &o.Mt[(size_t)e * nn], nn * sizeof(double));
 }

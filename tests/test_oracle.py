@@ -384,6 +384,8 @@ def test_high_order_matrices_on_affine_cells(dim, p):
 
     Gm, Mm = o.element_matrices(0)
     assert np.max(np.abs(Mm - kron_axes([m1] * dim) * vol)) < 1e-14
+    # the MassIntegrator mass of time absorption and scattering: the same integral
+    assert np.max(np.abs(o.time_mass(0) - kron_axes([m1] * dim) * vol)) < 1e-14
     # G_d(i, j) = -int phi_j d_d phi_i = -(vol / h_d) * (int l'_i l_j along d) * masses across
     for d in range(dim):
         mats = [d1 if k == d else m1 for k in range(dim)]
