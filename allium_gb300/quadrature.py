@@ -1,4 +1,6 @@
-"""Angular quadratures for the sweep: level-symmetric (LQn) sets and 1D Gauss-Legendre.
+"""Angular quadratures for the sweep: level-symmetric (LQn) sets, 1D Gauss-Legendre,
+product sets (Gauss-Legendre or Gauss-Lobatto polar levels x Chebyshev azimuths) and
+the rotation of a set.
 
 allium reads its level-symmetric sets from tables (src/angular_quadrature.cpp:98-147,
 data/lsquad/LS_N.txt).  Here the same sets are generated from the LQn construction:
@@ -162,3 +164,84 @@ def legendre_1d(order: int) -> AngularQuadrature:
 def single_angle(quad: AngularQuadrature, angle: int) -> AngularQuadrature:
     """SingleAngleQuadratureRule (angular_quadrature.hpp:45-56): one direction, weight 4 pi."""
     return AngularQuadrature(quad.dim, quad.omega[angle:angle + 1].copy(), np.array([4.0 * math.pi]))
+
+
+def _gauss_lobatto01(n: int):
+    """n-point Gauss-Lobatto rule on [0, 1] (ascending nodes, weights sum to 1)."""
+    if n < 2:
+        raise ValueError("Gauss-Lobatto needs at least 2 points")
+    if n == 2:
+        return np.array([0.0, 1.0]), np.array([0.5, 0.5])
+    # interior nodes: roots of P'_{n-1}; weights 2 / (n (n - 1) P_{n-1}(x)^2) on [-1, 1]
+    pn1 = np.polynomial.legendre.Legendre.basis(n - 1)
+    inner = np.sort(pn1.deriv().roots().real)
+    x = np.concatenate([[-1.0], inner, [1.0]])
+    w = 2.0 / (n * (n - 1) * pn1(x) ** 2)
+    return 0.5 * (x + 1.0), 0.5 * w
+
+
+def product(dim: int, polar: int, azimuthal: int, polar_type: str = "legendre",
+            triangular: bool = False) -> AngularQuadrature:
+    """ProductQuadrature (angular_quadrature.cpp:190-264): `polar` levels
+    theta_l = acos(2 x_l - 1) at the Gauss-Legendre (or Gauss-Lobatto, whose
+    end levels are the poles with one direction each) points x_l of [0, 1] in
+    ascending order; on level l, N_l azimuths phi_c = pi (2c + 1) / (2 N_l),
+    c = 0..N_l-1, with N_l = azimuthal, or 2, 3, .. up to the equator and back
+    when triangular.  Omega = (cos theta, sin theta cos phi[, sin theta sin phi]);
+    in 3D the reference's loop over two half-ranges computes the same azimuths
+    both times, so every 3D direction appears twice, kept here so that psi
+    vectors index the same set; weights scale * w_l * pi / N_l with scale 4 (2D)
+    or 2 (3D), so they sum to 4 pi."""
+    if dim not in (2, 3):
+        raise ValueError("product quadratures are 2D or 3D")
+    if polar_type == "legendre":
+        xg, wg = np.polynomial.legendre.leggauss(polar)
+        x, w = 0.5 * (xg + 1.0), 0.5 * wg
+        poles = False
+    elif polar_type == "lobatto":
+        x, w = _gauss_lobatto01(polar)
+        poles = True
+    else:
+        raise ValueError("polar_type is 'legendre' or 'lobatto'")
+    theta = np.arccos(2.0 * x - 1.0)
+    mid = polar // 2
+    if triangular:
+        # as the reference fills them: 2, 3, .. for the first half, mirrored for
+        # the second; with an odd level count the last level keeps no azimuths
+        levels = [i + 2 for i in range(mid)]
+        levels = levels + levels[::-1] + [0] * (polar - 2 * mid)
+    else:
+        levels = [azimuthal] * polar
+    if poles:
+        levels[0] = levels[-1] = 1
+    scale = 4.0 if dim == 2 else 2.0
+    dirs, wts = [], []
+    for lvl in range(polar):
+        naz = levels[lvl]
+        for _ in range(1 if dim == 2 else 2):
+            for c in range(naz):
+                phi = math.pi * (2 * (c + 1) - 1) / 2 / naz
+                om = [math.cos(theta[lvl]), math.sin(theta[lvl]) * math.cos(phi)]
+                if dim == 3:
+                    om.append(math.sin(theta[lvl]) * math.sin(phi))
+                dirs.append(om)
+                wts.append(scale * w[lvl] * math.pi / naz)
+    return AngularQuadrature(dim, np.array(dirs, dtype=np.float64), np.array(wts, dtype=np.float64))
+
+
+def rotate(quad: AngularQuadrature, x: float, y: float, z: float) -> AngularQuadrature:
+    """AngularQuadrature::Rotate (angular_quadrature.cpp:38-80): every direction
+    (lifted to 3D with its positive third component in 2D) multiplied by
+    R = Rx(x) Ry(y) Rz(z), then cut back to the set's dimension."""
+    if quad.dim == 1:
+        raise ValueError("rotation needs a 2D or 3D set")
+    cx, sx, cy, sy, cz, sz = math.cos(x), math.sin(x), math.cos(y), math.sin(y), math.cos(z), math.sin(z)
+    Rx = np.array([[1.0, 0.0, 0.0], [0.0, cx, -sx], [0.0, sx, cx]])
+    Ry = np.array([[cy, 0.0, sy], [0.0, 1.0, 0.0], [-sy, 0.0, cy]])
+    Rz = np.array([[cz, -sz, 0.0], [sz, cz, 0.0], [0.0, 0.0, 1.0]])
+    R = Rx @ Ry @ Rz
+    om = quad.omega
+    if quad.dim == 2:
+        om = np.column_stack([om, np.sqrt(np.clip(1.0 - (om * om).sum(1), 0.0, None))])
+    out = om @ R.T
+    return AngularQuadrature(quad.dim, np.ascontiguousarray(out[:, :quad.dim]), quad.weights.copy())

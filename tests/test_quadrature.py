@@ -67,3 +67,62 @@ def test_disjoint_union():
     assert u.num_vertices == a.num_vertices + b.num_vertices
     assert np.array_equal(u.elements[6:], b.elements + a.num_vertices)
     assert np.array_equal(u.boundary_attributes, np.concatenate([a.boundary_attributes, b.boundary_attributes]))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("polar,azimuthal,ptype,tri", [(4, 4, "legendre", False), (6, 3, "legendre", False),
+                                                       (5, 4, "lobatto", False), (6, 6, "legendre", True),
+                                                       (5, 5, "legendre", True)])
+def test_product_quadrature(dim, polar, azimuthal, ptype, tri):
+    # ProductQuadrature (angular_quadrature.cpp:190-264)
+    q = Q.product(dim, polar, azimuthal, ptype, tri)
+    mid = polar // 2
+    if tri:
+        levels = [i + 2 for i in range(mid)] + [i + 2 for i in range(mid)][::-1] + [0] * (polar - 2 * mid)
+    else:
+        levels = [azimuthal] * polar
+    if ptype == "lobatto":
+        levels[0] = levels[-1] = 1
+    assert q.size == sum(levels) * (2 if dim == 3 else 1)
+    if dim == 3:
+        assert np.allclose((q.omega ** 2).sum(1), 1.0, atol=1e-14)
+    else:
+        assert np.all((q.omega ** 2).sum(1) <= 1.0 + 1e-14)
+    if tri and polar % 2:
+        # the reference leaves the last level of an odd triangular set empty
+        assert levels[-1] == 0
+        return
+    assert abs(q.sum_weights() - 4 * np.pi) < 1e-12
+    # first moments vanish (symmetric polar points, azimuths symmetric about pi/2)
+    assert np.max(np.abs(q.weights @ q.omega[:, :2])) < 1e-12
+    if ptype == "lobatto":
+        assert np.isclose(q.omega[0, 0], -1.0) and np.isclose(q.omega[-1, 0], 1.0)
+    # polar levels in ascending Omega_x
+    assert np.all(np.diff(q.omega[:, 0]) >= -1e-15)
+
+
+def test_product_quadrature_polar_rule():
+    # the polar points are the Gauss rule on [0, 1]: sum_l w_l (2 x_l - 1)^2 = 1/3 exactly
+    q = Q.product(2, 8, 4)
+    assert abs(q.weights @ q.omega[:, 0] ** 2 - 4 * np.pi / 3) < 1e-12
+    lob_x, lob_w = Q._gauss_lobatto01(5)
+    assert abs(lob_w.sum() - 1.0) < 1e-15 and lob_x[0] == 0.0 and lob_x[-1] == 1.0
+    # Lobatto with n points integrates degree 2n - 3 exactly
+    assert abs(lob_w @ lob_x ** 7 - 1.0 / 8) < 1e-14
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rotate(dim):
+    # AngularQuadrature::Rotate (angular_quadrature.cpp:38-80): directions stay unit
+    # vectors, weights are kept, and a rotation by zero is the identity
+    q = Q.level_symmetric(6, dim)
+    r = Q.rotate(q, 0.3, -0.2, 0.7)
+    assert np.array_equal(r.weights, q.weights)
+    if dim == 3:
+        assert np.allclose((r.omega ** 2).sum(1), 1.0, atol=1e-14)
+        # the second moment tensor of a level-symmetric set is (4 pi / 3) I: rotation invariant
+        assert np.allclose((r.omega * r.weights[:, None]).T @ r.omega, 4 * np.pi / 3 * np.eye(3), atol=1e-12)
+    z = Q.rotate(q, 0.0, 0.0, 0.0)
+    assert np.allclose(z.omega, q.omega, atol=1e-15)
+    with pytest.raises(ValueError):
+        Q.rotate(Q.legendre_1d(4), 0.1, 0.0, 0.0)
