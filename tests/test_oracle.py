@@ -435,3 +435,13 @@ def test_transport_source_on_affine_cells(p):
         if ox > 0:   # enters through x = 0: DOFs with ix = 0, weight |Omega_x| * 2 * int l_iy
             want[0::n1] = ox * 2.0 * s1
         assert np.max(np.abs(srcb[a, 0] - want)) < 1e-14
+
+
+@pytest.mark.parametrize("dim,cells", [(2, (6, 5)), (3, (4, 3, 3))])
+def test_constant_solution_product_sets(dim, cells):
+    # test_sweep.cpp:7-108 with product sets (pole directions included) and a rotated set
+    mesh = M.cartesian(cells)
+    for quad in (Q.product(dim, 4, 4), Q.product(dim, 5, 3, "lobatto"), Q.rotate(Q.product(dim, 4, 4), 0.2, 0.1, 0.3)):
+        o = OracleSweep(mesh, 1, quad, np.zeros((1, mesh.num_elements)))
+        psi = o.mult(o.form_source(inflow=np.ones((1, 8))))
+        assert np.max(np.abs(psi - 1.0)) < 1e-12
