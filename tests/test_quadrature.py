@@ -126,3 +126,23 @@ def test_rotate(dim):
     assert np.allclose(z.omega, q.omega, atol=1e-15)
     with pytest.raises(ValueError):
         Q.rotate(Q.legendre_1d(4), 0.1, 0.0, 0.0)
+
+
+def _quadratic(om):
+    return 2 * om[:, 0] ** 2 + om[:, 1] ** 2 + om[:, 0] * om[:, 1]
+
+
+@pytest.mark.parametrize("tri", [True, False])
+@pytest.mark.parametrize("ptype", ["legendre", "lobatto"])
+def test_product_quadratic_known_answer(tri, ptype):
+    # test_angle_quad.cpp:137-151: sum w (2 Ox^2 + Oy^2 + Ox Oy) = 4 pi, 2D, orders 4..12
+    for order in range(4, 14, 2):
+        q = Q.product(2, order, order, ptype, tri)
+        assert abs(q.weights @ _quadratic(q.omega) - 4 * np.pi) < 1e-11
+
+
+def test_rotate_known_answers():
+    # test_angle_quad.cpp:153-173: the same integral after Rotate(pi/2, pi/4, pi/4)
+    for q in (Q.level_symmetric(4, 2), Q.product(2, 4, 6)):
+        r = Q.rotate(q, np.pi / 2, np.pi / 4, np.pi / 4)
+        assert abs(r.weights @ _quadratic(r.omega) - 4 * np.pi) < 1e-11
