@@ -69,6 +69,17 @@ EXPORTS = {
     "allium_sweep_mult_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_scattering_source_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_moments_f32_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_isotropic_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]),
+    "allium_sweep_fused_mult_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                              C.c_void_p, C.c_void_p]),
+    "allium_sweep_fused_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "allium_sweep_set_fused_pdl": (C.c_int, [C.c_void_p, C.c_int]),
+    "allium_sweep_transport_residual_df": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_moments_df": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_to_fused_layout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_from_fused_layout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_levels": (C.c_int, [C.c_void_p, C.c_void_p]),
     "allium_sweep_selftest_wait": (C.c_int, [C.c_void_p, C.c_int]),
     "allium_planck_spectrum": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_void_p]),

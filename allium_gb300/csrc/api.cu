@@ -67,6 +67,7 @@ int check_status(Handle& h) {
 
 void free_all(Handle& h) {
     allium::drop_graphs(h);
+    allium::free_fused(h);
     if (h.capture_stream) cudaStreamDestroy(h.capture_stream);
     for (cudaEvent_t ev : h.chunk_events)
         if (ev) cudaEventDestroy(ev);
@@ -606,6 +607,102 @@ int allium_sweep_moments_f32_nodes(allium_sweep* s, const float* psi, double* ph
     Handle& h = s->h;
     if (int st = device_only(h, {psi, phi}, "allium_sweep_moments_f32_nodes")) return st;
     CUDA_OR_FAIL(h, allium::launch_moments_nodes(h, psi, phi));
+    return ALLIUM_OK;
+}
+
+static int fused_check(Handle& h, const char* who) {
+    if (!allium::fused_supported(h)) {
+        h.last_error = std::string(who) + ": orders 0 and 1 with inflow or vacuum boundaries only";
+        return ALLIUM_ERR_UNSUPPORTED;
+    }
+    return ALLIUM_OK;
+}
+
+int allium_sweep_isotropic_source(allium_sweep* s, const double* sigma_s, const double* phi, const double* q_iso,
+                                  float* out, float* out_hi, float* out_lo) {
+    if (!s || (!out && !out_hi) || (!out_hi != !out_lo)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {phi, q_iso, out, out_hi, out_lo}, "allium_sweep_isotropic_source")) return st;
+    if (phi) {
+        int st = ensure_mass2(h);
+        if (st) return st;
+        if (sigma_s) {
+            st = upload(h, sigma_s, (size_t)h.G * h.ne, &h.d_sigma_s);
+            if (st) return st;
+        } else if (!h.d_sigma_s) {
+            h.last_error = "allium_sweep_isotropic_source: no scattering cross sections given yet";
+            return ALLIUM_ERR_ARG;
+        }
+    }
+    CUDA_OR_FAIL(h, allium::launch_iso_source(h, h.d_sigma_s, phi, q_iso, out, out_hi, out_lo));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_fused_mult_f32(allium_sweep* s, const float* iso, const float* source, float* psi, double* phi,
+                                int phi_mode, float* psi_hi, float* psi_lo) {
+    if (!s || !psi || phi_mode < 0 || phi_mode > 2 || (phi_mode && !phi) || (!psi_hi != !psi_lo)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = fused_check(h, "allium_sweep_fused_mult_f32")) return st;
+    if (int st = device_only(h, {iso, source, psi, phi, psi_hi, psi_lo}, "allium_sweep_fused_mult_f32")) return st;
+    if (misaligned(source ? source : psi, psi, true, true) || misaligned(iso ? iso : psi, psi_hi ? psi_hi : psi, true, true)) {
+        h.last_error = "device vectors must be 16-byte aligned";
+        return ALLIUM_ERR_ARG;
+    }
+    CUDA_OR_FAIL(h, allium::launch_fused_sweep(h, iso, source, psi, phi, phi_mode, psi_hi, psi_lo));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_fused_levels(allium_sweep* s, int* num_levels, int* unit_levels) {
+    if (!s || !num_levels || !unit_levels) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = fused_check(h, "allium_sweep_fused_levels")) return st;
+    CUDA_OR_FAIL(h, allium::fused_levels(h, num_levels, unit_levels));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_set_fused_pdl(allium_sweep* s, int on) {
+    if (!s) return ALLIUM_ERR_ARG;
+    allium::set_fused_pdl(s->h, on);
+    return ALLIUM_OK;
+}
+
+int allium_sweep_transport_residual_df(allium_sweep* s, const float* iso_hi, const float* iso_lo, const float* q_hi,
+                                       const float* q_lo, const float* psi_hi, const float* psi_lo, float* r) {
+    if (!s || !iso_hi || !iso_lo || !psi_hi || !psi_lo || !r || (!q_hi != !q_lo)) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = fused_check(h, "allium_sweep_transport_residual_df")) return st;
+    if (int st = device_only(h, {iso_hi, iso_lo, q_hi, q_lo, psi_hi, psi_lo, r}, "allium_sweep_transport_residual_df"))
+        return st;
+    if (misaligned(psi_hi, psi_lo, true, true) || misaligned(r, r, true, true)) {
+        h.last_error = "device vectors must be 16-byte aligned";
+        return ALLIUM_ERR_ARG;
+    }
+    CUDA_OR_FAIL(h, allium::launch_residual_df(h, iso_hi, iso_lo, q_hi, q_lo, psi_hi, psi_lo, r));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_moments_df(allium_sweep* s, const float* psi_hi, const float* psi_lo, double* phi) {
+    if (!s || !psi_hi || !psi_lo || !phi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = fused_check(h, "allium_sweep_moments_df")) return st;
+    if (int st = device_only(h, {psi_hi, psi_lo, phi}, "allium_sweep_moments_df")) return st;
+    CUDA_OR_FAIL(h, allium::launch_moments_df(h, psi_hi, psi_lo, phi));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_to_fused_layout(allium_sweep* s, const double* psi_right, float* hi, float* lo) {
+    if (!s || !psi_right || !hi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {psi_right, hi, lo}, "allium_sweep_to_fused_layout")) return st;
+    CUDA_OR_FAIL(h, allium::launch_fused_layout(h, 1, psi_right, hi, lo));
+    return ALLIUM_OK;
+}
+
+int allium_sweep_from_fused_layout(allium_sweep* s, const float* hi, const float* lo, double* psi_right) {
+    if (!s || !psi_right || !hi) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = device_only(h, {psi_right, hi, lo}, "allium_sweep_from_fused_layout")) return st;
+    CUDA_OR_FAIL(h, allium::launch_fused_layout(h, 0, psi_right, const_cast<float*>(hi), const_cast<float*>(lo)));
     return ALLIUM_OK;
 }
 

@@ -12,6 +12,8 @@
 
 namespace allium {
 
+struct FusedState;   // fused FP32 sweep and double-float residual (fused.cu)
+
 constexpr int kMaxOrder = 3;
 constexpr int kMaxRule = 5;   // largest 1D rule used (p + 2 points, p <= 3)
 
@@ -153,8 +155,13 @@ struct Handle {
     int* d_tile_count = nullptr;
     int ntiles = 0;
 
+    // fused FP32 inner sweep and double-float residual (fused.cu), built on first use
+    FusedState* fused = nullptr;
+
     std::string last_error;
 };
+
+void drop_fused_graphs(Handle& h);
 
 // Launch `body(stream)` through a cached CUDA graph keyed by (kind, src, dst):
 // captured once on a private stream, replayed on h.stream afterwards.
@@ -196,6 +203,7 @@ inline void drop_graphs(Handle& h) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = Handle::GraphEntry{};
     }
+    drop_fused_graphs(h);
 }
 
 // kernel error bits (d_status)
@@ -273,6 +281,21 @@ cudaError_t launch_scatter_nodes(Handle& h, const double* sigma_s, const double*
 cudaError_t launch_moments_nodes(Handle& h, const float* psi, double* phi);
 bool factor_cache_supported(const Handle& h);
 cudaError_t ensure_factors(Handle& h);
+
+// ---- fused FP32 inner sweep, isotropic source, double-float residual (fused.cu)
+// psi-sized vectors in the fused layout v[((g Ne + e) Nw + a) n + i]
+bool fused_supported(const Handle& h);
+void free_fused(Handle& h);
+void set_fused_pdl(Handle& h, int on);
+cudaError_t fused_levels(Handle& h, int* num_levels, int* unit_levels);
+cudaError_t launch_fused_sweep(Handle& h, const float* iso, const float* src, float* psi, double* phi, int phi_mode,
+                               float* acc_hi, float* acc_lo);
+cudaError_t launch_iso_source(Handle& h, const double* sigma_s, const double* phi, const double* q_iso, float* out,
+                              float* out_hi, float* out_lo);
+cudaError_t launch_residual_df(Handle& h, const float* iso_hi, const float* iso_lo, const float* q_hi, const float* q_lo,
+                               const float* psi_hi, const float* psi_lo, float* r);
+cudaError_t launch_moments_df(Handle& h, const float* hi, const float* lo, double* phi);
+cudaError_t launch_fused_layout(Handle& h, int to_fused, const double* right, float* hi, float* lo);
 
 }  // namespace allium
 

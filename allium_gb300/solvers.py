@@ -13,7 +13,10 @@ src/transport_op.hpp:9-35).  Provided here:
   T (the Krylov option of chive);
 * refine: FP32-inner / FP64-outer iterative refinement.  The outer residual
   r = b - T phi uses the FP64 sweep; each correction solves T d = r with GMRES
-  whose operator applies the FP32 sweep (moments accumulated in FP64); phi += d.
+  whose operator applies the FP32 sweep (moments accumulated in FP64); phi += d;
+* refine_fused: the same refinement on the transport system with no FP64 sweep:
+  psi kept in double-float, the residual q + D^T S D psi - L psi evaluated in
+  double-float arithmetic, every sweep the fused FP32 operator.
 
 All vectors are torch float64 CUDA tensors of length G * Ndof (phi) or
 G * Nw * Ndof (psi).  Diffusion synthetic acceleration (allium_gb300.dsa) is
@@ -260,6 +263,121 @@ def refine_rhs(op, b, x0=None, tol=1e-8, inner_tol=1e-4, restart=30, max_outer=2
     torch.cuda.synchronize()
     res = SolveResult(phi, outer, conv, hist, time.perf_counter() - t0, op.sweeps64, op.sweeps32)
     res.inner_iterations = inner_total
+    return res
+
+
+class FusedSchur:
+    """T = I - D L^{-1} D^T S with the fused FP32 sweep: per application one small
+    kernel builds the per-cell source (S x)/sum(w) and one CUDA graph sweeps
+    (one launch per wavefront level) and sums D psi (allium_sweep_fused_mult_f32);
+    psi stays in a scratch vector of the fused layout."""
+
+    def __init__(self, Linv: InverseAdvectionOperator, sigma_s):
+        self.L = Linv
+        dev = torch.device("cuda")
+        self.sigma_s = torch.as_tensor(np.ascontiguousarray(sigma_s, dtype=np.float64).reshape(-1), device=dev)
+        self.n = Linv.G * Linv.ndof
+        self.iso = torch.empty(self.n, dtype=torch.float32, device=dev)
+        self.psi32 = torch.empty(Linv.width, dtype=torch.float32, device=dev)
+        self.tmp = torch.empty(self.n, dtype=torch.float64, device=dev)
+        self.sweeps32 = 0
+
+    def apply32(self, x, out):
+        self.L.IsotropicSource(self.sigma_s, x, None, out=self.iso)
+        self.L.FusedMultF32(self.iso, None, self.psi32, phi=self.tmp, phi_mode=1)
+        self.sweeps32 += 1
+        torch.sub(x, self.tmp, out=out)
+        return out
+
+
+def split_isotropic(Linv: InverseAdvectionOperator, q):
+    """(q_iso, q_rest) for a psi-sized RIGHT source q: q_iso [G*Ndof] when q is the
+    same in every direction (FormTransportSource of an isotropic density with
+    vacuum boundaries), else (None, q)."""
+    v = q.view(Linv.G, Linv.Nw, Linv.ndof)
+    q0 = v[:, :1, :]
+    if bool(torch.all(v == q0).item()):
+        return q0.reshape(-1).contiguous(), None
+    return None, q
+
+
+def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, tol=1e-8, inner_tol=1e-4, restart=30,
+                 max_outer=20, inner_maxiter=500, prec=None):
+    """FP32-inner / FP64-outer refinement on the transport system itself,
+    L psi - D^T S D psi = q, with no FP64 sweep.
+
+    psi is kept as a double-float pair (hi + lo, about 48 bits).  Each outer step
+    takes the residual r = q + D^T S phi - L psi in double-float arithmetic
+    (allium_sweep_transport_residual_df, phi = D psi), projects it with one FP32
+    sweep, rho = D L^{-1} r, which is the residual b - T phi of the scalar-flux
+    system T phi = b = D L^{-1} q (exe/chive.cpp:704-735) that the FP64 solvers
+    iterate on, solves T d = rho by GMRES on the fused FP32 operator, and
+    corrects psi += L^{-1} (r + D^T S d) with one more FP32 sweep; phi = D psi
+    is then summed from the double-float psi.  Stops when ||rho|| <= tol ||rho_0||.
+    q is the psi-sized RIGHT FP64 source (a CUDA tensor) or q_iso its per-cell
+    part when it is the same in every direction.  Returns a SolveResult whose
+    phi is the FP64 scalar flux."""
+    t0 = time.perf_counter()
+    L = Linv
+    dev = torch.device("cuda")
+    fs = FusedSchur(L, sigma_s)
+    W, n = L.width, fs.n
+    q_rest = None
+    if q_iso is None:
+        q_iso, q_rest = split_isotropic(L, q)
+    q_hi = q_lo = None
+    if q_rest is not None:
+        q_hi = torch.empty(W, dtype=torch.float32, device=dev)
+        q_lo = torch.empty(W, dtype=torch.float32, device=dev)
+        L.ToFusedLayout(q_rest, q_hi, q_lo)
+    hi = torch.zeros(W, dtype=torch.float32, device=dev)
+    lo = torch.zeros(W, dtype=torch.float32, device=dev)
+    r32 = torch.empty(W, dtype=torch.float32, device=dev)
+    phi = torch.zeros(n, dtype=torch.float64, device=dev)
+    rho = torch.empty(n, dtype=torch.float64, device=dev)
+    iso_hi = torch.empty(n, dtype=torch.float32, device=dev)
+    iso_lo = torch.empty(n, dtype=torch.float32, device=dev)
+    # rho_0 = D L^{-1} q (the residual of psi = 0)
+    if q_iso is not None:
+        L.IsotropicSource(None, None, q_iso, out=fs.iso)
+    L.FusedMultF32(fs.iso if q_iso is not None else None, q_hi, fs.psi32, phi=rho, phi_mode=1)
+    fs.sweeps32 += 1
+    r0 = torch.linalg.norm(rho).item()
+    hist, outer, inner_total, conv, residuals = [], 0, 0, False, 0
+    if r0 == 0.0:
+        res = SolveResult(phi, 0, True, [0.0], time.perf_counter() - t0, 0, fs.sweeps32)
+        res.inner_iterations, res.residuals_df = 0, 0
+        return res
+    while outer <= max_outer:
+        rn = torch.linalg.norm(rho).item()
+        hist.append(rn / r0)
+        if rn <= tol * r0:
+            conv = True
+            break
+        if outer == max_outer:
+            break
+        # enough accuracy to land below tol in this step, never looser than needed
+        eta = max(inner_tol, 0.5 * tol * r0 / rn)
+        d, it, _ = gmres(fs.apply32, rho, tol=eta, restart=restart, maxiter=inner_maxiter, prec=prec)
+        inner_total += it
+        # psi += L^{-1} (r + D^T S d); phi = D psi in double-float (FP32 moment
+        # sums of the correction would leave phi 1e-7 away from D psi)
+        L.IsotropicSource(fs.sigma_s, d, q_iso if outer == 0 else None, out=fs.iso)
+        L.FusedMultF32(fs.iso, q_hi if outer == 0 else r32, fs.psi32, acc=(hi, lo))
+        fs.sweeps32 += 1
+        L.MomentsDF(hi, lo, phi)
+        # r = q + D^T S phi - L psi (double-float), rho = D L^{-1} r
+        L.IsotropicSource(fs.sigma_s, phi, q_iso, out_hi=iso_hi, out_lo=iso_lo)
+        L.TransportResidualDF(iso_hi, iso_lo, hi, lo, r32, q_hi, q_lo)
+        residuals += 1
+        L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=1)
+        fs.sweeps32 += 1
+        outer += 1
+    torch.cuda.synchronize()
+    res = SolveResult(phi, outer, conv, hist, time.perf_counter() - t0, 0, fs.sweeps32)
+    res.inner_iterations = inner_total
+    res.residuals_df = residuals
+    res.psi = (hi, lo)
     return res
 
 

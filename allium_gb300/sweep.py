@@ -176,6 +176,92 @@ class InverseAdvectionOperator:
                                                            C.c_void_p(_ptr(psi, np.float64, self.width, "psi"))), self.h)
         return psi
 
+    # --- fused FP32 inner operator and the double-float residual (device tensors;
+    # psi-sized vectors in the fused layout v[((g*Ne + e)*Nw + a)*n + i])
+    def FusedMultF32(self, iso, source, psi, phi=None, phi_mode=0, acc=None):
+        """psi = L^{-1} (iso + source) in FP32 with phi = D psi (phi_mode 1) or
+        phi += D psi (2) in the same graph; acc = (hi, lo) double-float
+        accumulator that psi is added to.  iso [G*Ndof] float32 per-cell source
+        or None, source psi-sized float32 or None."""
+        nd = self.G * self.ndof
+        ip = _ptr(iso, np.float32, nd, "iso") if iso is not None else None
+        sp = _ptr(source, np.float32, self.width, "source") if source is not None else None
+        fp = _ptr(phi, np.float64, nd, "phi") if phi is not None else None
+        hp = _ptr(acc[0], np.float32, self.width, "acc_hi") if acc is not None else None
+        lp = _ptr(acc[1], np.float32, self.width, "acc_lo") if acc is not None else None
+        check(_lib.lib().allium_sweep_fused_mult_f32(self.h, C.c_void_p(ip), C.c_void_p(sp),
+                                                     C.c_void_p(_ptr(psi, np.float32, self.width, "psi")),
+                                                     C.c_void_p(fp), int(phi_mode), C.c_void_p(hp), C.c_void_p(lp)),
+              self.h)
+        return psi
+
+    def FusedLevels(self):
+        """(number of levels, 1 if they are unit levels else 0) of the fused sweep's schedule."""
+        n, u = C.c_int(), C.c_int()
+        check(_lib.lib().allium_sweep_fused_levels(self.h, C.byref(n), C.byref(u)), self.h)
+        return n.value, u.value
+
+    def SetFusedPDL(self, on):
+        """1: the fused sweep's level launches overlap (programmatic dependent launch); 0: plain order."""
+        check(_lib.lib().allium_sweep_set_fused_pdl(self.h, int(on)), self.h)
+
+    def IsotropicSource(self, sigma_s, phi, q_iso=None, out=None, out_hi=None, out_lo=None):
+        """Per-cell source (sigma_s M phi)/sum(w) + q_iso in FP64, written as float32
+        (out) and/or double-float (out_hi, out_lo).  sigma_s [G, Ne] numpy or
+        float64 CUDA tensor, or None to reuse the last one; phi, q_iso float64
+        CUDA tensors [G*Ndof] or None."""
+        nd = self.G * self.ndof
+        sp = None
+        if sigma_s is not None:
+            if torch is not None and isinstance(sigma_s, torch.Tensor):
+                sp = _ptr(sigma_s, np.float64, self.G * self.mesh.num_elements, "sigma_s")
+            else:
+                sig = np.ascontiguousarray(sigma_s, dtype=np.float64).reshape(self.G, -1)
+                self._sigma_s_keep = sig
+                sp = sig.ctypes.data
+        args = [sp, _ptr(phi, np.float64, nd, "phi") if phi is not None else None,
+                _ptr(q_iso, np.float64, nd, "q_iso") if q_iso is not None else None,
+                _ptr(out, np.float32, nd, "out") if out is not None else None,
+                _ptr(out_hi, np.float32, nd, "out_hi") if out_hi is not None else None,
+                _ptr(out_lo, np.float32, nd, "out_lo") if out_lo is not None else None]
+        check(_lib.lib().allium_sweep_isotropic_source(self.h, *[C.c_void_p(a) for a in args]), self.h)
+
+    def TransportResidualDF(self, iso_hi, iso_lo, psi_hi, psi_lo, r, q_hi=None, q_lo=None):
+        """r = q + D^T S phi - L psi in double-float arithmetic, stored as float32."""
+        nd = self.G * self.ndof
+        W = self.width
+        args = [_ptr(iso_hi, np.float32, nd, "iso_hi"), _ptr(iso_lo, np.float32, nd, "iso_lo"),
+                _ptr(q_hi, np.float32, W, "q_hi") if q_hi is not None else None,
+                _ptr(q_lo, np.float32, W, "q_lo") if q_lo is not None else None,
+                _ptr(psi_hi, np.float32, W, "psi_hi"), _ptr(psi_lo, np.float32, W, "psi_lo"),
+                _ptr(r, np.float32, W, "r")]
+        check(_lib.lib().allium_sweep_transport_residual_df(self.h, *[C.c_void_p(a) for a in args]), self.h)
+        return r
+
+    def MomentsDF(self, hi, lo, phi):
+        """phi = D (hi + lo) for a fused-layout double-float psi, FP64 out."""
+        check(_lib.lib().allium_sweep_moments_df(
+            self.h, C.c_void_p(_ptr(hi, np.float32, self.width, "hi")),
+            C.c_void_p(_ptr(lo, np.float32, self.width, "lo")),
+            C.c_void_p(_ptr(phi, np.float64, self.G * self.ndof, "phi"))), self.h)
+        return phi
+
+    def ToFusedLayout(self, psi, hi, lo=None):
+        """RIGHT float64 psi -> fused-layout float32 hi (and its remainder lo)."""
+        check(_lib.lib().allium_sweep_to_fused_layout(
+            self.h, C.c_void_p(_ptr(psi, np.float64, self.width, "psi")),
+            C.c_void_p(_ptr(hi, np.float32, self.width, "hi")),
+            C.c_void_p(_ptr(lo, np.float32, self.width, "lo") if lo is not None else None)), self.h)
+        return hi
+
+    def FromFusedLayout(self, hi, lo, psi):
+        """fused-layout float32 hi (+ lo) -> RIGHT float64 psi."""
+        check(_lib.lib().allium_sweep_from_fused_layout(
+            self.h, C.c_void_p(_ptr(hi, np.float32, self.width, "hi")),
+            C.c_void_p(_ptr(lo, np.float32, self.width, "lo") if lo is not None else None),
+            C.c_void_p(_ptr(psi, np.float64, self.width, "psi"))), self.h)
+        return psi
+
     RIGHT, LEFT = 0, 1
 
     def Relayout(self, x, x_layout, out, out_layout):

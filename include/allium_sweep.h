@@ -292,6 +292,72 @@ int allium_sweep_scattering_source_f32_nodes(allium_sweep* s, const double* sigm
                                              const float* q_nodes, float* out);
 int allium_sweep_moments_f32_nodes(allium_sweep* s, const float* psi, double* phi);
 
+/* ---- fused FP32 inner operator and the FP64-accurate transport residual ----
+ * The pieces of an FP32-inner / FP64-outer solve that never needs an FP64
+ * sweep (device vectors only; orders 0 and 1, inflow or vacuum boundaries,
+ * else ALLIUM_ERR_UNSUPPORTED).  psi-sized vectors use the fused layout
+ *     v[((g*Ne + e)*Nw + a)*n + i]
+ * (group, cell, angle, DOF), equal to the node-major layout when G = 1; a
+ * "double-float" vector is a pair of FP32 vectors hi, lo whose sum carries
+ * about 48 bits (hi = fl32(x), lo = fl32(x - hi)). */
+
+/* Per-cell isotropic source s[g][e n + i] = (sigma_s (M phi))/sum(w) + q_iso: the
+ * D^T (S phi) + q of chive's source build (exe/chive.cpp:593-599,
+ * MomentMethodFixedPointOperator::Mult, src/transport_op.hpp:75-90) for a source
+ * q that is the same in every direction (FormTransportSource of an isotropic
+ * density with vacuum boundaries), computed in FP64 and written as FP32 (out)
+ * and/or double-float (out_hi, out_lo).  phi and q_iso are [G][Ndof] FP64 and
+ * may each be NULL; sigma_s [G][Ne] (host or device) is required with phi the
+ * first time, NULL reuses the last one given. */
+int allium_sweep_isotropic_source(allium_sweep* s, const double* sigma_s, const double* phi, const double* q_iso,
+                                  float* out, float* out_hi, float* out_lo);
+
+/* The inner operator phi = D L^{-1} (iso + source) as one CUDA graph:
+ * InverseAdvectionOperator::Mult (src/sweep.cpp:277-669) in FP32, one launch per
+ * wavefront level, with the isotropic source read per cell (iso [G][Ndof], or
+ * NULL) plus an optional psi-sized FP32 source, followed by
+ * DiscreteToMoment::Mult (src/transport_op.cpp:3-31) of the FP32 psi summed in
+ * double-float arithmetic: phi_mode 0 leaves phi alone, 1 writes phi = D psi,
+ * 2 adds D psi to phi (FP64).  psi receives the FP32 angular flux;
+ * psi_hi/psi_lo (or NULL) is a double-float vector that psi is added to.
+ * source may equal psi. */
+int allium_sweep_fused_mult_f32(allium_sweep* s, const float* iso, const float* source, float* psi, double* phi,
+                                int phi_mode, float* psi_hi, float* psi_lo);
+
+/* Wavefront levels of the fused sweep (no reference counterpart; the reference
+ * sweeps node frontiers, src/sweep.cpp:308-322).  The fused sweep orders whole
+ * units -- a cell's angles with the same octant and face pattern, which read
+ * their upwind traces across the same faces -- by Kahn frontiers of the unit
+ * graph, so all of a unit's angles share a level (unit_levels = 1); if that
+ * graph has a cycle it keeps the node levels (unit_levels = 0).  Either order
+ * sweeps every node after its upwind nodes. */
+int allium_sweep_fused_levels(allium_sweep* s, int* num_levels, int* unit_levels);
+
+/* Launch overlap of the fused sweep's level launches (no reference
+ * counterpart): 1 (default) lets each level's blocks start while the previous
+ * level drains (programmatic dependent launch; they load their records, cell
+ * tables and sources, then wait before reading upwind traces), 0 plain
+ * stream order.  Results do not depend on it. */
+int allium_sweep_set_fused_pdl(allium_sweep* s, int on);
+
+/* r = q + D^T S phi - L psi for a double-float psi: AdvectionOperator::Mult
+ * (src/sweep.cpp:1246-1387) subtracted from the source, evaluated in
+ * double-float arithmetic on the FP32 units (error-free products and sums, about
+ * 1e-14 of |q|), written as FP32 r.  iso_hi/iso_lo is the per-cell part
+ * (allium_sweep_isotropic_source of phi and q_iso), q_hi/q_lo an optional
+ * psi-sized part of q. */
+int allium_sweep_transport_residual_df(allium_sweep* s, const float* iso_hi, const float* iso_lo, const float* q_hi,
+                                       const float* q_lo, const float* psi_hi, const float* psi_lo, float* r);
+
+/* DiscreteToMoment::Mult (src/transport_op.cpp:3-31) of a double-float psi in the
+ * fused layout, summed in double-float arithmetic: phi[G][Ndof] (FP64) to about
+ * 1e-14 of sum_a w_a |psi_a|. */
+int allium_sweep_moments_df(allium_sweep* s, const float* psi_hi, const float* psi_lo, double* phi);
+
+/* RIGHT FP64 <-> fused-layout double-float (lo may be NULL: FP32 only) */
+int allium_sweep_to_fused_layout(allium_sweep* s, const double* psi_right, float* hi, float* lo);
+int allium_sweep_from_fused_layout(allium_sweep* s, const float* hi, const float* lo, double* psi_right);
+
 /* Wavefront level of every (cell, angle) node e*Nw + a (the Kahn frontier
  * index of src/sweep.cpp:308-512), host or device int array [Ne*Nw]. */
 int allium_sweep_levels(allium_sweep* s, int* levels);
