@@ -255,6 +255,20 @@ __device__ __forceinline__ void ld_vec(const float* p, float (&r)[N]) {
     }
 }
 
+template <int N>
+__device__ __forceinline__ void st_vec(float* p, const float (&r)[N]) {
+    if constexpr (N % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < N / 4; ++c)
+            reinterpret_cast<float4*>(p)[c] = make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]);
+    } else if constexpr (N == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = r[i];
+    }
+}
+
 // the same through the L2 only (data written by other SMs in an earlier launch)
 template <int N>
 __device__ __forceinline__ void ld_vec_cg(const float* p, float (&r)[N]) {
@@ -893,26 +907,22 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
             x[k] = v * rinv[k];
         });
         if (!ok) atomicOr(f.status, kErrSingular);
-        float* out = f.psi + idx;
-        if constexpr (N % 4 == 0) {
-#pragma unroll
-            for (int i = 0; i < N; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
-        } else {
-#pragma unroll
-            for (int i = 0; i < N; ++i) out[i] = x[i];
-        }
+        st_vec<N>(f.psi + idx, x);
         if (f.acc_hi) {
-            float* ph = f.acc_hi + idx;
-            float* pl = f.acc_lo + idx;
+            // (hi, lo) += x: TwoSum into hi, the rounding error into lo
+            float h[N], l[N];
+            ld_vec<N>(f.acc_hi + idx, h);
+            ld_vec<N>(f.acc_lo + idx, l);
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-                const float h = ph[i];
-                const float s = __fadd_rn(h, x[i]);
-                const float bv = __fsub_rn(s, h);
-                const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bv)), __fsub_rn(x[i], bv));
-                ph[i] = s;
-                pl[i] = __fadd_rn(pl[i], err);
+                const float s = __fadd_rn(h[i], x[i]);
+                const float bv = __fsub_rn(s, h[i]);
+                const float err = __fadd_rn(__fsub_rn(h[i], __fsub_rn(s, bv)), __fsub_rn(x[i], bv));
+                h[i] = s;
+                l[i] = __fadd_rn(l[i], err);
             }
+            st_vec<N>(f.acc_hi + idx, h);
+            st_vec<N>(f.acc_lo + idx, l);
         }
     });
 }

@@ -82,6 +82,32 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def fp64_fma_peak(reps=3):
+    """FP64 multiply-add rate of this GPU (G DFMA/s), measured with the library's
+    probe kernel: every SM full of threads running independent FMA chains."""
+    import ctypes as C
+    import torch
+    from allium_gb300 import _lib
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    sink = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    run = lambda: _lib.check(_lib.lib().allium_fp64_fma_probe(blocks, threads, iters, C.c_void_p(sink.data_ptr()),
+                                                               C.c_void_p(st.cuda_stream)))
+    run()
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        run()
+        e1.record(st)
+        e1.synchronize()
+        best = max(best, blocks * threads * 8.0 * iters / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    return {"gdfma_s": best, "tflops": 2e-3 * best, "blocks": blocks, "threads": threads,
+            "fma_per_thread": 8 * iters}
+
+
 def traffic_per_entry():
     """DRAM bytes per swept entry of the FP64 sweep kernel from the committed
     ncu summary (profiles/sweep_fp64_traffic.json), or None."""
@@ -214,13 +240,17 @@ def cpu_extrapolated(line, rate3d, n3d):
     return out
 
 
-def solve_section(L, mesh, quad, sigma, src, maxiter=400):
+def solve_section(L, mesh, quad, sigma, src, maxiter=400, fp64_setup_s=0.0, fused_setup_s=0.0):
     """Time to a 1e-8 relative residual of T phi = b on the 3D workload with
     sigma_s / sigma_t ~ U[0.5, 0.999] per cell: FP64 GMRES(30) with the FP64
-    sweep against FP32-inner / FP64-outer refinement, each without and with
-    MIP-DSA as the right preconditioner."""
+    sweep against FP32-inner / FP64-outer refinement (the fused FP32 operator
+    with double-float residuals and no FP64 sweep; and the earlier form whose
+    outer residuals are FP64 sweeps), each without and with MIP-DSA as the
+    right preconditioner.  fp64_setup_s / fused_setup_s: the one-off setup of
+    each arm (the FP64 factor pass; the fused schedule and FP32 cell tables),
+    added in the *_with_setup figures."""
     import torch
-    from allium_gb300.solvers import SchurOperator, refine, solve_gmres, true_residual
+    from allium_gb300.solvers import SchurOperator, refine, refine_fused, solve_gmres, true_residual
     rng = np.random.default_rng(SEED + 2)
     sigma_s = sigma * rng.uniform(0.5, 0.999, size=sigma.shape)
     # operator setup shared by both: stored FP64 and FP32 local inverses
@@ -244,6 +274,21 @@ def solve_section(L, mesh, quad, sigma, src, maxiter=400):
                                     "residual": true_residual(op2, b, ir.phi)}
     out["speedup"] = plain.seconds / ir.seconds if ir.seconds > 0 else None
     out["phi_rel_diff"] = float((torch.max(torch.abs(ir.phi - plain.phi)) / torch.max(torch.abs(plain.phi))).item())
+    # the fused FP32 operator with double-float residuals: no FP64 sweep at all
+    refine_fused(L, sigma_s, src, tol=1e-8)   # warm-up (graphs of its buffers)
+    torch.cuda.synchronize()
+    fr = refine_fused(L, sigma_s, src, tol=1e-8, inner_tol=1e-4, restart=30)
+    del fr.psi
+    out["fp32_fused_refinement"] = {
+        "seconds": fr.seconds, "outer": fr.iterations, "inner_iterations": fr.inner_iterations,
+        "converged": fr.converged, "fp64_sweeps": fr.sweeps64, "fp32_sweeps": fr.sweeps32,
+        "double_float_residuals": fr.residuals_df, "history": fr.history, "residual": true_residual(op2, b, fr.phi),
+        "phi_rel_diff_vs_fp64_gmres": float((torch.max(torch.abs(fr.phi - plain.phi))
+                                             / torch.max(torch.abs(plain.phi))).item())}
+    out["fused_speedup"] = plain.seconds / fr.seconds
+    out["setup_seconds"] = {"fp64_factor_pass": fp64_setup_s, "fused_schedule_and_tables": fused_setup_s}
+    out["fused_speedup_with_setup"] = (plain.seconds + fp64_setup_s) / (fr.seconds + fused_setup_s)
+    torch.cuda.empty_cache()
     # MIP-DSA as the right preconditioner of both (inexact block-Jacobi CG inside)
     from allium_gb300.dsa import DSAPreconditioner
     t0 = time.perf_counter()
@@ -609,6 +654,40 @@ def run_gpu(args):
     err32n = float((torch.max(torch.abs(back - psi)) / torch.max(torch.abs(psi))).item())
     del f_src, f_psi, back
 
+    # --- fused FP32 inner operator: phi = D L^-1 (D^T S x / sum w) on the fused layout
+    nd = L.G * L.ndof
+    t0 = time.perf_counter()
+    fused_levels = L.FusedLevels()          # schedule setup (unit levels, records)
+    iso = torch.rand(nd, dtype=torch.float32, device="cuda")
+    fz_psi = torch.empty(N, dtype=torch.float32, device="cuda")
+    fz_phi = torch.empty(nd, dtype=torch.float64, device="cuda")
+    L.FusedMultF32(iso, None, fz_psi, phi=fz_phi, phi_mode=1)   # FP32 cell tables, graph capture
+    torch.cuda.synchronize()
+    fused_setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        L.FusedMultF32(iso, None, fz_psi, phi=fz_phi, phi_mode=1)
+    L.synchronize()
+    ms_fused = _timed(stream, args.steps, lambda i: L.FusedMultF32(iso, None, fz_psi, phi=fz_phi, phi_mode=1))
+    ms_fused_nophi = _timed(stream, args.steps, lambda i: L.FusedMultF32(iso, None, fz_psi))
+    # accuracy of the fused sweep on the headline source against the FP64 sweep
+    fz_src = torch.empty(N, dtype=torch.float32, device="cuda")
+    L.ToFusedLayout(srcs[0], fz_src)
+    L.FusedMultF32(None, fz_src, fz_psi)
+    back = torch.empty_like(psi)
+    L.FromFusedLayout(fz_psi, None, back)
+    L.Mult(srcs[0], psi)
+    L.synchronize()
+    err_fused = float((torch.max(torch.abs(back - psi)) / torch.max(torch.abs(psi))).item())
+    # double-float residual and moments
+    hi_t = fz_psi.clone()
+    lo_t = torch.zeros_like(hi_t)
+    iso_lo = torch.zeros_like(iso)
+    r32 = torch.empty_like(fz_psi)
+    ms_resid = _timed(stream, max(3, args.steps // 4), lambda i: L.TransportResidualDF(iso, iso_lo, hi_t, lo_t, r32))
+    ms_mom_df = _timed(stream, max(3, args.steps // 4), lambda i: L.MomentsDF(hi_t, lo_t, fz_phi))
+    del fz_src, back, hi_t, lo_t, r32, fz_psi
+    torch.cuda.empty_cache()
+
     # --- e2e through the C ABI with pinned host buffers (copies inside the timed region)
     h_srcs = [s.cpu().pin_memory() for s in srcs]
     h_psi = torch.empty_like(h_srcs[0]).pin_memory()
@@ -637,6 +716,7 @@ def run_gpu(args):
         return
 
     peak, peak_kind = measured_peaks()
+    fp64_peak = fp64_fma_peak()
     alg_bytes = 16.0 * N + 8.0 * mesh.num_elements * (1 + 3 * 8)
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     tpe = traffic_per_entry()
@@ -661,20 +741,21 @@ def run_gpu(args):
                                                for t in pipe["trials"]}}},
             "gpu_launches": args.steps * (L.num_levels if tuned["fp64"]["schedule"] == 0 else 2),
             "roofline": roof,
-            # the kernel's own bound: GB300's FP64 pipe (1.25 TFLOP/s nominal = 625 G DFMA/s);
-            # per (cell, angle) node of the p = 1 hex sweep: 64 DFMA for inv(A) b plus 20 per
-            # inflow face (F u and its scaling), 3 inflow faces on average
+            # the kernel's own bound: GB300's FP64 pipe, its multiply-add rate measured in
+            # this run (fp64_fma_peak); per (cell, angle) node of the p = 1 hex sweep: 64 DFMA
+            # for inv(A) b plus 20 per inflow face (F u and its scaling), 3 inflow faces on average
             "fp64_pipe": {"achieved_gdfma_s": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9,
-                          "peak_gdfma_s": 625.0, "peak_kind": "nominal",
-                          "frac": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9 / 625.0},
+                          "peak_gdfma_s": fp64_peak["gdfma_s"], "peak_kind": "measured",
+                          "peak_probe": fp64_peak,
+                          "frac": (N / 8) * (64 + 3 * 20) / (ms * 1e-3) / 1e9 / fp64_peak["gdfma_s"]},
             # the same bound in the units of a flop roofline: flops executed per DOF*angle
             # (2 per DFMA) against the reference algorithm's (per-node assembly and LU,
             # about 211 for 3D p = 1), whose work the stored inverses avoid
             "compute_roofline": {"executed_flops_per_unit": 2.0 * (64 + 3 * 20) / 8,
                                  "reference_algorithm_flops_per_unit": 211,
                                  "achieved_tflops": N * 2.0 * (64 + 3 * 20) / 8 / (ms * 1e-3) / 1e12,
-                                 "peak_tflops": 1.25, "peak_kind": "nominal FP64",
-                                 "frac": N * 2.0 * (64 + 3 * 20) / 8 / (ms * 1e-3) / 1e12 / 1.25,
+                                 "peak_tflops": 2e-3 * fp64_peak["gdfma_s"], "peak_kind": "measured FP64 FMA rate",
+                                 "frac": N * 2.0 * (64 + 3 * 20) / 8 / (ms * 1e-3) / 1e12 / (2e-3 * fp64_peak["gdfma_s"]),
                                  "reference_algorithm_equivalent_tflops": N * 211 / (ms * 1e-3) / 1e12},
             "fp64_uncached": {"value": N / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                               "note": "every Mult assembles and factors all local systems (pivoted LU), as the reference does"},
@@ -691,10 +772,26 @@ def run_gpu(args):
                            "max_rel_err_vs_fp64": err32n,
                            "roofline_frac": (8.0 * N / (ms32n * 1e-3) / 1e9) / peak,
                            "note": "node-major layout (the refinement's inner sweep), from an FP32 copy of the stored inverses"},
+            "fp32_fused": {
+                "value": N / (ms_fused * 1e-3), "unit": UNIT, "ms_per_step": ms_fused,
+                "ms_without_moments": ms_fused_nophi, "max_rel_err_vs_fp64": err_fused,
+                "levels": fused_levels[0], "unit_levels": bool(fused_levels[1]), "setup_seconds": fused_setup_s,
+                "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
+                             "algorithmic_bytes_per_entry": 8,
+                             "achieved": 8.0 * N / (ms_fused * 1e-3) / 1e9,
+                             "frac": 8.0 * N / (ms_fused * 1e-3) / 1e9 / peak},
+                "kernels": "k_fused_level<3,1> once per level + k_moments_f32, one CUDA graph",
+                "note": ("the inner operator phi = D L^-1 (D^T S x / sum w) of the refinement: per-cell source "
+                         "in registers, FP32 local solves, moments in double-float; 8 B per entry is the "
+                         "FP32 sweep's algorithmic traffic (read q, write psi)")},
+            "double_float_residual_ms": ms_resid,
+            "double_float_moments_ms": ms_mom_df,
             "clocks": clk.summary()}
     if not args.no_solve:
         warm_solver_libraries()
-        line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0])
+        line["time_to_tolerance"] = solve_section(L, mesh, quad, sigma, srcs[0],
+                                                  fp64_setup_s=max(0.0, (ms_first - ms) * 1e-3),
+                                                  fused_setup_s=fused_setup_s)
         line["chive_2d"] = chive2d_section(cpu=not args.no_cpu)
         line["trt_marshak"] = trt_section(args.trt_steps)
         line["learned_iterate"] = learned_section(args.trt_steps, min(50, args.trt_steps // 4))

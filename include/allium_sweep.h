@@ -500,6 +500,14 @@ int allium_mlp_adam(long long count, float* w, void* w_bf16, const float* grad, 
 /* y = bf16(x). */
 int allium_mlp_to_bf16(long long count, const float* x, void* y, void* stream);
 
+/* FP64 multiply-add throughput probe (no reference counterpart): blocks x
+ * threads threads each run 8 independent FMA chains for iters steps on the
+ * given cudaStream_t (2 * 8 * iters flops per thread); the caller times it.
+ * sink is a device buffer of blocks * threads doubles that is written only if
+ * the chains reach an impossible value.  The measured rate is the bound of
+ * the FP64 sweep, whose work is multiply-adds. */
+int allium_fp64_fma_probe(int blocks, int threads, long long iters, double* sink, void* stream);
+
 /* Wait for the handle's stream; report sticky kernel errors and clear them. */
 int allium_sweep_synchronize(allium_sweep* s);
 
