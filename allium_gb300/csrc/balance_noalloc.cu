@@ -1,11 +1,10 @@
 // allium_sweep_balance_noalloc: the balance reduction for callers that cannot
 // allocate GPU memory at the point of the call.
 //
-// Who needs it: code that calls the library while a CUDA stream is being
-// captured into a graph (cudaMalloc is not allowed during capture), code that
-// runs under a caller-owned memory pool or a real-time time-step loop where
-// allocating is forbidden, and embedded uses where the host runtime hands the
-// library only the vectors it works on.  allium_sweep_balance itself needs no
+// Who needs it: code that runs under a caller-owned memory pool or in a
+// real-time time-step loop where allocating is forbidden (an allocation would
+// synchronise the device or exceed the caller's budget), and embedded uses
+// where the host runtime hands the library only the vectors it works on.  allium_sweep_balance itself needs no
 // allocation on a device pointer either, but it relies on a partial-sum buffer
 // that the handle allocated; this variant keeps its partial sums in a
 // file-scope device array instead.
@@ -14,7 +13,9 @@
 // device image, so every GPU that loads the library holds it until the
 // process exits.  Its device address is looked up with cudaGetSymbolAddress
 // the first time the entry point runs on a device (with that device current);
-// make that first call before any stream capture begins.  All calls share the
+// make that first call before any stream capture begins.  The address is kept
+// per device index for the process, which assumes one CUDA context per device
+// for the library's lifetime.  All calls share the
 // array: each call writes every partial it later reads and the result slot,
 // so nothing has to be cleared between calls, but two calls whose kernels
 // overlap on the GPU (different streams, or different handles on one device)

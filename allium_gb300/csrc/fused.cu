@@ -785,13 +785,17 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
         for (int k = 0; k < NFACE; ++k)
             if (((pat >> (2 * k)) & 3) == 2) nb[k] = f.nbr[(size_t)e * NFACE + k];
     }
-    // the upwind traces were written by earlier levels
+    // the upwind traces were written by earlier levels: fold each inflow face's
+    // term |Omega.n| F_k u_k into b as its trace arrives (the face block and
+    // normal through L1 from the cell's table, which the warp shares), so that
+    // no trace stays live across the table wait
     griddep_wait();
-    float u[NFACE][NF];
     if (valid) {
+        const float* gt = f.tab + (size_t)e * T::size;
         sfor<0, NFACE>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
             if (((pat >> (2 * k)) & 3) == 2) {
+                float u[NF];
                 const float* up = f.psi + fused_index(f.ne, f.Nw, N, g, nb[k] >> 1, a);
                 if (nb[k] & 1) {
                     // standard DOF map: the neighbour's face k^1 DOFs, picked at compile time
@@ -799,44 +803,47 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
                     ld_vec_cg<N>(up, blk);
                     sfor<0, NF>([&](auto jc) {
                         constexpr int jj = decltype(jc)::value;
-                        u[k][jj] = blk[face_dof(D, P, k ^ 1, jj)];
+                        u[jj] = blk[face_dof(D, P, k ^ 1, jj)];
                     });
                 } else {
                     const unsigned m4 = f.map[(size_t)e * NFACE + k];
 #pragma unroll
-                    for (int jj = 0; jj < NF; ++jj) u[k][jj] = __ldcg(up + ((m4 >> (8 * jj)) & 0xffu));
+                    for (int jj = 0; jj < NF; ++jj) u[jj] = __ldcg(up + ((m4 >> (8 * jj)) & 0xffu));
                 }
+                const float4 nr = __ldg(reinterpret_cast<const float4*>(gt + T::oNrm + 4 * k));
+                float d = om.x * nr.x;
+                if (D > 1) d = fmaf(om.y, nr.y, d);
+                if (D > 2) d = fmaf(om.z, nr.z, d);
+                d = fabsf(d);
+                sfor<0, NF>([&](auto ic) {
+                    constexpr int ii = decltype(ic)::value;
+                    float fr[NF];
+                    ld_vec<NF>(gt + T::oF + (k * NF + ii) * NF, fr);
+                    float acc = 0.f;
+#pragma unroll
+                    for (int jj = 0; jj < NF; ++jj) acc = fmaf(fr[jj], u[jj], acc);
+                    constexpr int fi = face_dof(D, P, k, ii);
+                    b[fi] = fmaf(d, acc, b[fi]);
+                });
             }
         });
     }
 
     for_each_round<kSlots>(wtab, wbar, f.tab, T::size, valid, run, start, e, f.status, [&](unsigned tb) {
         const float omv[3] = {om.x, om.y, om.z};
+        // |Omega.n| on the outflow faces
         float dk[NFACE];
 #pragma unroll
         for (int k = 0; k < NFACE; ++k) {
-            const float4 nr = lds4(tb + 4u * (T::oNrm + 4 * k));
-            float d = omv[0] * nr.x;
-            if (D > 1) d = fmaf(omv[1], nr.y, d);
-            if (D > 2) d = fmaf(omv[2], nr.z, d);
-            dk[k] = fabsf(d);
-        }
-        // right-hand side: b += |Omega.n| F_k u_k on the inflow faces
-        sfor<0, NFACE>([&](auto kc) {
-            constexpr int k = decltype(kc)::value;
-            if (((pat >> (2 * k)) & 3) == 2) {
-                sfor<0, NF>([&](auto ic) {
-                    constexpr int ii = decltype(ic)::value;
-                    float fr[NF];
-                    lds_vec<NF>(tb + 4u * (T::oF + (k * NF + ii) * NF), fr);
-                    float acc = 0.f;
-#pragma unroll
-                    for (int jj = 0; jj < NF; ++jj) acc = fmaf(fr[jj], u[k][jj], acc);
-                    constexpr int fi = face_dof(D, P, k, ii);
-                    b[fi] = fmaf(dk[k], acc, b[fi]);
-                });
+            dk[k] = 0.f;
+            if (((pat >> (2 * k)) & 3) == 1) {
+                const float4 nr = lds4(tb + 4u * (T::oNrm + 4 * k));
+                float d = omv[0] * nr.x;
+                if (D > 1) d = fmaf(omv[1], nr.y, d);
+                if (D > 2) d = fmaf(omv[2], nr.z, d);
+                dk[k] = fabsf(d);
             }
-        });
+        }
         // rows of A = sum_d Omega_d G_d + sigma M [+ tau Mt] + sum_{outflow} |Omega.n| F_k,
         // assembled one at a time and eliminated against the rows above (no pivoting);
         // only the upper triangle U and the reciprocal pivots stay live
@@ -1093,8 +1100,11 @@ __global__ void __launch_bounds__(kFusedBlock, 4) k_residual_df(ResidArgs f) {
         for (int p = 0; p < NP; ++p)
             y[p] = {make_float2(yr[2 * p].hi, 2 * p + 1 < N ? yr[2 * p + 1].hi : 0.f),
                     make_float2(yr[2 * p].lo, 2 * p + 1 < N ? yr[2 * p + 1].lo : 0.f)};
-#pragma unroll
+        // a rolled loop over the columns (psi_j re-read from L1): the unrolled
+        // double-float body would not fit the instruction cache
+#pragma unroll 1
         for (int j = 0; j < N; ++j) {
+            const dd xj = {f.psi_hi[idx + j], f.psi_lo[idx + j]};
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
                 dd2 c = {f2(0.f), f2(0.f)};
@@ -1104,7 +1114,7 @@ __global__ void __launch_bounds__(kFusedBlock, 4) k_residual_df(ResidArgs f) {
                     const dd2 m = {lds2(th + o), lds2(tl + o)};
                     dd2_acc(c, dd2_prod(m, cf[v]));
                 }
-                dd2_acc(y[p], dd2_prod(dd2_norm(c), x[j]));
+                dd2_acc(y[p], dd2_prod(dd2_norm(c), xj));
             }
         }
 #pragma unroll

@@ -137,11 +137,15 @@ def source_iteration(op: SchurOperator, q, tol=1e-8, maxiter=10000, phi0=None, d
     return SolveResult(phi, it, conv, hist, time.perf_counter() - t0, op.sweeps64, op.sweeps32)
 
 
-def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=None):
+def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=None, final_residual=True):
     """Restarted GMRES on torch vectors; stops when ||b - A x|| <= max(tol ||b||, atol)
     (the Arnoldi residual estimate).  prec(v, out) is a right preconditioner,
     kept in flexible form (the preconditioned directions are stored), so it
-    may be an inner iterative solve.  Returns (x, iterations, history)."""
+    may be an inner iterative solve.  With final_residual the residual of the
+    iterate is recomputed with one more application of A after each cycle
+    (restart or stop); without it the last cycle that meets the tolerance ends on
+    the Arnoldi estimate (for inner solves whose caller checks the residual
+    itself).  Returns (x, iterations, history)."""
     dev, n = b.device, b.numel()
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     bnorm = torch.linalg.norm(b).item()
@@ -201,6 +205,8 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=
         y = np.linalg.solve(np.triu(H[:k_used, :k_used]), g[:k_used])
         basis = Z if prec is not None else V
         x += torch.mv(basis[:k_used].t(), torch.from_numpy(y).to(dev))
+        if not final_residual and abs(g[k_used]) <= target:
+            break
         apply(x, w)
         r = b - w
         beta = torch.linalg.norm(r).item()
@@ -358,7 +364,8 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
             break
         # enough accuracy to land below tol in this step, never looser than needed
         eta = max(inner_tol, 0.5 * tol * r0 / rn)
-        d, it, _ = gmres(fs.apply32, rho, tol=eta, restart=restart, maxiter=inner_maxiter, prec=prec)
+        d, it, _ = gmres(fs.apply32, rho, tol=eta, restart=restart, maxiter=inner_maxiter, prec=prec,
+                         final_residual=False)
         inner_total += it
         # psi += L^{-1} (r + D^T S d); phi = D psi in double-float (FP32 moment
         # sums of the correction would leave phi 1e-7 away from D psi)

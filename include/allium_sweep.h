@@ -206,17 +206,20 @@ int allium_sweep_apply_L(allium_sweep* s, const double* x, double* y);
 int allium_sweep_balance(allium_sweep* s, const double* psi, double* out);
 
 /* The balance of allium_sweep_balance for callers that cannot allocate GPU
- * memory at the time of the call: code recording a CUDA graph by stream
- * capture (where cudaMalloc is not allowed), code running under its own memory
- * pool or in a time-step loop that must not allocate, and hosts that hand the
- * library only the vectors it works on.  No counterpart in the reference.
- * It allocates nothing: psi must be device memory, *out may be device or host
- * memory (a host *out makes the call wait for the result).  Its partial sums
+ * memory at the time of the call: code running under its own memory pool or
+ * in a time-step loop that must not allocate (an allocation there would
+ * synchronise the device or break the caller's memory budget), and hosts that
+ * hand the library only the vectors it works on.  No counterpart in the
+ * reference.  It allocates nothing: psi must be device memory, *out may be
+ * device or host memory (a host *out makes the call copy the result to the
+ * host and wait for it).  Its partial sums
  * live in a fixed 32 KB array inside the library's device image, held by every
  * GPU that loads the library until the process exits, which limits it to
  * G*Nw*Ne <= 134217728 items (larger problems get ALLIUM_ERR_SIZE).  The first
  * call on each device looks the array up (cudaGetSymbolAddress) with that
- * device current: make it before any stream capture starts.  Calls share the
+ * device current: make it before any stream capture starts.  The address is
+ * kept for the rest of the process, so the library assumes one CUDA context
+ * per device for its lifetime (no cudaDeviceReset in between).  Calls share the
  * array, so calls whose kernels overlap on the GPU race; results match
  * allium_sweep_balance to rounding (the partial sums are grouped differently). */
 int allium_sweep_balance_noalloc(allium_sweep* s, const double* psi, double* out);

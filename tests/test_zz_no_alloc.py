@@ -1,6 +1,6 @@
 """allium_sweep_balance_noalloc, the entry point for callers that cannot
-allocate GPU memory when they call (stream capture, caller-owned memory pools,
-allocation-free time steps).  Called through the C ABI and checked against
+allocate GPU memory when they call (caller-owned memory pools, allocation-free
+time steps, hosts that hand the library only its vectors).  Called through the C ABI and checked against
 allium_sweep_balance, with the 1e-12 relative tolerance of the other FP64
 tests, on two calls in a row.  Collected last so that a failure here comes
 after every other test has run."""
