@@ -78,6 +78,7 @@ EXPORTS = {
     "allium_sweep_transport_residual_df": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                      C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_moments_df": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_sweep_transport_residual_update_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_to_fused_layout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_from_fused_layout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_levels": (C.c_int, [C.c_void_p, C.c_void_p]),

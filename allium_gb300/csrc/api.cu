@@ -681,6 +681,20 @@ int allium_sweep_transport_residual_df(allium_sweep* s, const float* iso_hi, con
     return ALLIUM_OK;
 }
 
+int allium_sweep_transport_residual_update_f32(allium_sweep* s, const float* iso, const float* dpsi, float* r) {
+    if (!s || !iso || !dpsi || !r) return ALLIUM_ERR_ARG;
+    Handle& h = s->h;
+    if (int st = fused_check(h, "allium_sweep_transport_residual_update_f32")) return st;
+    if (int st = device_only(h, {iso, dpsi, r}, "allium_sweep_transport_residual_update_f32")) return st;
+    if (misaligned(iso, dpsi, true, true) || misaligned(r, r, true, true)) {
+        h.last_error = "device vectors must be 16-byte aligned";
+        return ALLIUM_ERR_ARG;
+    }
+    if (!h.fp32_ready) CUDA_OR_FAIL(h, allium::make_fp32_copies(h));
+    CUDA_OR_FAIL(h, allium::launch_residual_update_f32(h, iso, dpsi, r));
+    return ALLIUM_OK;
+}
+
 int allium_sweep_moments_df(allium_sweep* s, const float* psi_hi, const float* psi_lo, double* phi) {
     if (!s || !psi_hi || !psi_lo || !phi) return ALLIUM_ERR_ARG;
     Handle& h = s->h;

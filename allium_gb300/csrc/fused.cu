@@ -784,6 +784,11 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
 #pragma unroll
         for (int k = 0; k < NFACE; ++k)
             if (((pat >> (2 * k)) & 3) == 2) nb[k] = f.nbr[(size_t)e * NFACE + k];
+        // the cell's face blocks and normals into L1 for the inflow fold below
+        // (griddepcontrol.wait is a compiler barrier, so those loads come after it)
+        const char* ft = reinterpret_cast<const char*>(f.tab + (size_t)e * T::size + T::oF);
+#pragma unroll
+        for (int off = 0; off < 4 * (T::size - T::oF); off += 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(ft + off));
     }
     // the upwind traces were written by earlier levels: fold each inflow face's
     // term |Omega.n| F_k u_k into b as its trace arrives (the face block and
@@ -1140,6 +1145,141 @@ __global__ void __launch_bounds__(kFusedBlock, 4) k_residual_df(ResidArgs f) {
 #pragma unroll
             for (int i = 0; i < N; ++i) out[i] = rv[i];
         }
+    });
+}
+
+// ---------------------------------------------------------------- FP32 residual update
+struct UpdateArgs {
+    int ne, Nw, G;
+    const float* tab;        // the sweep's FP32 cell tables
+    const Slot* slots;
+    const int* nbr;          // 2 * neighbour + standard-map bit
+    const unsigned* map;
+    const float* dots;       // [nfaces][Nw] FP32 Omega . n (sign of the FP64 value)
+    const float4* omega;
+    const float* sigma;      // [G][ne]
+    float tau;
+    const float* iso;        // [G][ne][N]: (S D x) / sum(w)
+    const float* x;          // fused layout
+    float* r;                // fused layout, r += iso - L x
+    int* status;
+};
+
+// r += iso - L x in FP32 for every (group, cell, angle) node, angle fastest:
+// the residual of psi + x from the residual r of psi, for a correction x small
+// against psi (its FP32 rounding is then small against r).
+template <int D, int P, bool TD>
+__global__ void __launch_bounds__(kFusedBlock) k_residual_update_f32(UpdateArgs f) {
+    using S = Shape<D, P>;
+    using T = Tab<D, P, TD>;
+    constexpr int N = S::N, NF = S::NF, NFACE = S::NFACE;
+    constexpr int NP = (N + 1) / 2;
+    __shared__ __align__(128) float s_tab[kFusedWarps * kSlots * T::size];
+    __shared__ __align__(8) unsigned long long s_bar[kFusedWarps * kSlots];
+    const int warp = threadIdx.x >> 5;
+    const long long total = (long long)f.G * f.ne * f.Nw;
+    const long long t = (long long)blockIdx.x * kFusedBlock + threadIdx.x;
+    const bool valid = t < total;
+    int g = 0, e = 0, a = 0;
+    if (valid) {
+        a = (int)(t % f.Nw);
+        const long long rr = t / f.Nw;
+        e = (int)(rr % f.ne);
+        g = (int)(rr / f.ne);
+    }
+    float* wtab = s_tab + warp * kSlots * T::size;
+    unsigned long long* wbar = s_bar + warp * kSlots;
+    bool start = false;
+    const int run = stage_runs<kSlots>(wtab, wbar, f.tab, T::size, valid, g * f.ne + e, e, start);
+    const long long idx = fused_index(f.ne, f.Nw, N, g, e, a);
+    float x[N], y[N];
+    float4 om = make_float4(0.f, 0.f, 0.f, 0.f);
+    float sg = 0.f;
+    if (valid) {
+        ld_vec<N>(f.x + idx, x);
+        om = f.omega[a];
+        sg = f.sigma[(size_t)g * f.ne + e];
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) y[i] = 0.f;
+    for_each_round<kSlots>(wtab, wbar, f.tab, T::size, valid, run, start, e, f.status, [&](unsigned tb) {
+        const float omv[3] = {om.x, om.y, om.z};
+        // volume part: row i of (sum_d Omega_d G_d + sigma M [+ tau Mt]) dotted with x
+        float2 xp[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) xp[p] = make_float2(x[2 * p], 2 * p + 1 < N ? x[2 * p + 1] : 0.f);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            float2 ar[NP], tr[NP];
+            lds_row<N>(tb + 4u * (T::oG + i * N), tr);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) ar[p] = mul2(f2(omv[0]), tr[p]);
+#pragma unroll
+            for (int d = 1; d < D; ++d) {
+                lds_row<N>(tb + 4u * (T::oG + d * N * N + i * N), tr);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) ar[p] = fma2(f2(omv[d]), tr[p], ar[p]);
+            }
+            lds_row<N>(tb + 4u * (T::oM + i * N), tr);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) ar[p] = fma2(f2(sg), tr[p], ar[p]);
+            if constexpr (TD) {
+                lds_row<N>(tb + 4u * (T::oMt + i * N), tr);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) ar[p] = fma2(f2(f.tau), tr[p], ar[p]);
+            }
+            float2 acc = mul2(ar[0], xp[0]);
+#pragma unroll
+            for (int p = 1; p < NP; ++p) acc = fma2(ar[p], xp[p], acc);
+            y[i] = acc.x + acc.y;
+        }
+        // face terms with Omega.n of the FP64 sign: outflow on x's own trace, inflow on the upwind x
+        sfor<0, NFACE>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            const Slot q = f.slots[(size_t)e * NFACE + k];
+            const float d1 = f.dots[(size_t)q.face * f.Nw + a];
+            const float dk = q.side ? -d1 : d1;
+            const bool out = dk > 0.f, in = dk < 0.f && q.nbr >= 0;
+            if (!out && !in) return;
+            float u[NF];
+            if (out) {
+                sfor<0, NF>([&](auto jc) {
+                    constexpr int jj = decltype(jc)::value;
+                    u[jj] = x[face_dof(D, P, k, jj)];
+                });
+            } else {
+                const int nbv = f.nbr[(size_t)e * NFACE + k];
+                const float* up = f.x + fused_index(f.ne, f.Nw, N, g, nbv >> 1, a);
+                if (nbv & 1) {
+                    float blk[N];
+                    ld_vec<N>(up, blk);
+                    sfor<0, NF>([&](auto jc) {
+                        constexpr int jj = decltype(jc)::value;
+                        u[jj] = blk[face_dof(D, P, k ^ 1, jj)];
+                    });
+                } else {
+                    const unsigned m4 = f.map[(size_t)e * NFACE + k];
+#pragma unroll
+                    for (int jj = 0; jj < NF; ++jj) u[jj] = up[(m4 >> (8 * jj)) & 0xffu];
+                }
+            }
+            sfor<0, NF>([&](auto ic) {
+                constexpr int ii = decltype(ic)::value;
+                float fr[NF];
+                lds_vec<NF>(tb + 4u * (T::oF + (k * NF + ii) * NF), fr);
+                float acc = 0.f;
+#pragma unroll
+                for (int jj = 0; jj < NF; ++jj) acc = fmaf(fr[jj], u[jj], acc);
+                constexpr int fi = face_dof(D, P, k, ii);
+                y[fi] = fmaf(dk, acc, y[fi]);
+            });
+        });
+        float r[N], s[N];
+        ld_vec<N>(f.r + idx, r);
+        ld_vec<N>(f.iso + ((long long)g * f.ne + e) * N, s);
+#pragma unroll
+        for (int i = 0; i < N; ++i) r[i] += s[i] - y[i];
+        st_vec<N>(f.r + idx, r);
     });
 }
 
@@ -1601,6 +1741,33 @@ cudaError_t launch_residual_df(Handle& h, const float* iso_hi, const float* iso_
         default: return cudaErrorNotSupported;
     }
 #undef RS_CASE
+}
+
+cudaError_t launch_residual_update_f32(Handle& h, const float* iso, const float* x, float* r) {
+    FusedState& fs = *fused_state(h);
+    FCK(prepare_common(h, fs));
+    if (!h.fp32_ready) FCK(make_fp32_copies(h));
+    const int td = h.time_dependent ? 1 : 0;
+    if (fs.tab_td != td) {
+        drop_fused_graphs(h);
+        FCK(dispatch_tab<false>(h, fs));
+    }
+    UpdateArgs a;
+    a.ne = h.ne; a.Nw = h.Nw; a.G = h.G;
+    a.tab = fs.tab; a.slots = h.d_slots; a.nbr = fs.nbr; a.map = fs.map; a.dots = h.f_dots;
+    a.omega = fs.omega; a.sigma = h.f_sigma; a.tau = (float)h.tau;
+    a.iso = iso; a.x = x; a.r = r; a.status = h.d_status;
+    const long long total = (long long)h.G * h.ne * h.Nw;
+#define UP_CASE(D_, P_)                                                                                          \
+    case D_ * 10 + P_:                                                                                           \
+        if (td) k_residual_update_f32<D_, P_, true><<<blocks(total, kFusedBlock), kFusedBlock, 0, h.stream>>>(a);  \
+        else k_residual_update_f32<D_, P_, false><<<blocks(total, kFusedBlock), kFusedBlock, 0, h.stream>>>(a);    \
+        return cudaGetLastError();
+    switch (h.dim * 10 + h.p) {
+        UP_CASE(1, 0) UP_CASE(1, 1) UP_CASE(2, 0) UP_CASE(2, 1) UP_CASE(3, 0) UP_CASE(3, 1)
+        default: return cudaErrorNotSupported;
+    }
+#undef UP_CASE
 }
 
 cudaError_t launch_moments_df(Handle& h, const float* hi, const float* lo, double* phi) {

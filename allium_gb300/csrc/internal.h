@@ -295,6 +295,7 @@ cudaError_t launch_iso_source(Handle& h, const double* sigma_s, const double* ph
 cudaError_t launch_residual_df(Handle& h, const float* iso_hi, const float* iso_lo, const float* q_hi, const float* q_lo,
                                const float* psi_hi, const float* psi_lo, float* r);
 cudaError_t launch_moments_df(Handle& h, const float* hi, const float* lo, double* phi);
+cudaError_t launch_residual_update_f32(Handle& h, const float* iso, const float* x, float* r);
 cudaError_t launch_fused_layout(Handle& h, int to_fused, const double* right, float* hi, float* lo);
 
 }  // namespace allium

@@ -308,7 +308,7 @@ def split_isotropic(Linv: InverseAdvectionOperator, q):
 
 
 def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, tol=1e-8, inner_tol=1e-4, restart=30,
-                 max_outer=20, inner_maxiter=500, prec=None):
+                 max_outer=20, inner_maxiter=500, prec=None, incremental=None):
     """FP32-inner / FP64-outer refinement on the transport system itself,
     L psi - D^T S D psi = q, with no FP64 sweep.
 
@@ -318,8 +318,13 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     sweep, rho = D L^{-1} r, which is the residual b - T phi of the scalar-flux
     system T phi = b = D L^{-1} q (exe/chive.cpp:704-735) that the FP64 solvers
     iterate on, solves T d = rho by GMRES on the fused FP32 operator, and
-    corrects psi += L^{-1} (r + D^T S d) with one more FP32 sweep; phi = D psi
-    is then summed from the double-float psi.  Stops when ||rho|| <= tol ||rho_0||.
+    corrects psi += L^{-1} (r + D^T S d) with one more FP32 sweep, whose graph
+    also sums D of the correction (double-float sums) into phi.  The first
+    residual is evaluated in double-float; later ones (incremental, the default
+    for tol >= 1e-10) are updated in FP32 from the previous one,
+    r += D^T S D dpsi - L dpsi, which is accurate to ~1e-7 of the previous
+    residual because the correction dpsi is small.  Stops when
+    ||rho|| <= tol ||rho_0||.
     q is the psi-sized RIGHT FP64 source (a CUDA tensor) or q_iso its per-cell
     part when it is the same in every direction.  Returns a SolveResult whose
     phi is the FP64 scalar flux."""
@@ -340,19 +345,22 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     lo = torch.zeros(W, dtype=torch.float32, device=dev)
     r32 = torch.empty(W, dtype=torch.float32, device=dev)
     phi = torch.zeros(n, dtype=torch.float64, device=dev)
+    dphi = torch.empty(n, dtype=torch.float64, device=dev)
     rho = torch.empty(n, dtype=torch.float64, device=dev)
     iso_hi = torch.empty(n, dtype=torch.float32, device=dev)
     iso_lo = torch.empty(n, dtype=torch.float32, device=dev)
+    if incremental is None:
+        incremental = tol >= 1e-10
     # rho_0 = D L^{-1} q (the residual of psi = 0)
     if q_iso is not None:
         L.IsotropicSource(None, None, q_iso, out=fs.iso)
     L.FusedMultF32(fs.iso if q_iso is not None else None, q_hi, fs.psi32, phi=rho, phi_mode=1)
     fs.sweeps32 += 1
     r0 = torch.linalg.norm(rho).item()
-    hist, outer, inner_total, conv, residuals = [], 0, 0, False, 0
+    hist, outer, inner_total, conv, residuals, updates = [], 0, 0, False, 0, 0
     if r0 == 0.0:
         res = SolveResult(phi, 0, True, [0.0], time.perf_counter() - t0, 0, fs.sweeps32)
-        res.inner_iterations, res.residuals_df = 0, 0
+        res.inner_iterations, res.residuals_df, res.residual_updates = 0, 0, 0
         return res
     while outer <= max_outer:
         rn = torch.linalg.norm(rho).item()
@@ -367,16 +375,22 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
         d, it, _ = gmres(fs.apply32, rho, tol=eta, restart=restart, maxiter=inner_maxiter, prec=prec,
                          final_residual=False)
         inner_total += it
-        # psi += L^{-1} (r + D^T S d); phi = D psi in double-float (FP32 moment
-        # sums of the correction would leave phi 1e-7 away from D psi)
+        # psi += dpsi = L^{-1} (r + D^T S d); phi += D dpsi (double-float sums)
         L.IsotropicSource(fs.sigma_s, d, q_iso if outer == 0 else None, out=fs.iso)
-        L.FusedMultF32(fs.iso, q_hi if outer == 0 else r32, fs.psi32, acc=(hi, lo))
+        L.FusedMultF32(fs.iso, q_hi if outer == 0 else r32, fs.psi32, phi=dphi, phi_mode=1, acc=(hi, lo))
         fs.sweeps32 += 1
-        L.MomentsDF(hi, lo, phi)
-        # r = q + D^T S phi - L psi (double-float), rho = D L^{-1} r
-        L.IsotropicSource(fs.sigma_s, phi, q_iso, out_hi=iso_hi, out_lo=iso_lo)
-        L.TransportResidualDF(iso_hi, iso_lo, hi, lo, r32, q_hi, q_lo)
-        residuals += 1
+        phi += dphi
+        if outer == 0 or not incremental:
+            # r = q + D^T S phi - L psi in double-float arithmetic
+            L.IsotropicSource(fs.sigma_s, phi, q_iso, out_hi=iso_hi, out_lo=iso_lo)
+            L.TransportResidualDF(iso_hi, iso_lo, hi, lo, r32, q_hi, q_lo)
+            residuals += 1
+        else:
+            # r += D^T S D dpsi - L dpsi in FP32
+            L.IsotropicSource(fs.sigma_s, dphi, None, out=fs.iso)
+            L.TransportResidualUpdateF32(fs.iso, fs.psi32, r32)
+            updates += 1
+        # rho = D L^{-1} r
         L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=1)
         fs.sweeps32 += 1
         outer += 1
@@ -384,6 +398,7 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     res = SolveResult(phi, outer, conv, hist, time.perf_counter() - t0, 0, fs.sweeps32)
     res.inner_iterations = inner_total
     res.residuals_df = residuals
+    res.residual_updates = updates
     res.psi = (hi, lo)
     return res
 

@@ -238,6 +238,14 @@ class InverseAdvectionOperator:
         check(_lib.lib().allium_sweep_transport_residual_df(self.h, *[C.c_void_p(a) for a in args]), self.h)
         return r
 
+    def TransportResidualUpdateF32(self, iso, dpsi, r):
+        """r += iso - L dpsi in FP32 (the residual after a small correction dpsi)."""
+        W = self.width
+        check(_lib.lib().allium_sweep_transport_residual_update_f32(
+            self.h, C.c_void_p(_ptr(iso, np.float32, self.G * self.ndof, "iso")),
+            C.c_void_p(_ptr(dpsi, np.float32, W, "dpsi")), C.c_void_p(_ptr(r, np.float32, W, "r"))), self.h)
+        return r
+
     def MomentsDF(self, hi, lo, phi):
         """phi = D (hi + lo) for a fused-layout double-float psi, FP64 out."""
         check(_lib.lib().allium_sweep_moments_df(

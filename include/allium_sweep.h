@@ -352,6 +352,14 @@ int allium_sweep_set_fused_pdl(allium_sweep* s, int on);
 int allium_sweep_transport_residual_df(allium_sweep* s, const float* iso_hi, const float* iso_lo, const float* q_hi,
                                        const float* q_lo, const float* psi_hi, const float* psi_lo, float* r);
 
+/* The residual of psi + dpsi from the residual r of psi, in FP32:
+ * r += iso - L dpsi (AdvectionOperator::Mult, src/sweep.cpp:1246-1387, of the
+ * correction; iso [G][Ndof] is the per-cell (S D dpsi)/sum(w) from
+ * allium_sweep_isotropic_source).  Its rounding is about 1e-7 of |L dpsi|, so
+ * it keeps r accurate while dpsi is small against psi; fused-layout FP32
+ * vectors. */
+int allium_sweep_transport_residual_update_f32(allium_sweep* s, const float* iso, const float* dpsi, float* r);
+
 /* DiscreteToMoment::Mult (src/transport_op.cpp:3-31) of a double-float psi in the
  * fused layout, summed in double-float arithmetic: phi[G][Ndof] (FP64) to about
  * 1e-14 of sum_a w_a |psi_a|. */

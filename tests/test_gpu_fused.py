@@ -235,3 +235,30 @@ def test_fused_rejects_unsupported():
     with pytest.raises(AlliumError) as e:
         L.FusedMultF32(None, psi, psi)
     assert e.value.status == 7
+
+
+@pytest.mark.parametrize("case", CASES + [CASES[6] + ("td",)], ids=IDS + [IDS[6] + "-td"])
+def test_residual_update_f32(case):
+    """From r = 0 the FP32 update gives D^T S D x - L x: the FP64 oracle's
+    scattering source of D x minus its forward operator, to FP32 accuracy."""
+    td = len(case) > 6
+    L, o = setup(case[:6], tau=3.0 if td else None)
+    rng = np.random.default_rng(10)
+    ne = L.mesh.num_elements
+    sigma_s = rng.uniform(0.1, 0.9, (L.G, ne))
+    x = rng.uniform(-1.0, 1.0, L.width)
+    ref = o.scattering_source(sigma_s, o.moments(x)) - o.apply_L(x)
+    xf = torch.tensor(fused_of_right(L, x), dtype=torch.float32, device="cuda")
+    phi = torch.empty(L.G * L.ndof, dtype=torch.float64, device="cuda")
+    xh = torch.empty(L.width, dtype=torch.float32, device="cuda")
+    L.ToFusedLayout(torch.tensor(x, device="cuda"), xh, torch.empty_like(xh))
+    assert torch.equal(xh, xf)
+    L.MomentsDF(xf, torch.zeros_like(xf), phi)
+    iso = torch.empty(L.G * L.ndof, dtype=torch.float32, device="cuda")
+    L.IsotropicSource(sigma_s, phi, None, out=iso)
+    r = torch.zeros_like(xf)
+    L.TransportResidualUpdateF32(iso, xf, r)
+    L.synchronize()
+    got = right_of_fused(L, r.cpu().numpy().astype(np.float64))
+    scale = max(np.max(np.abs(o.apply_L(np.abs(x)))), 1e-300)
+    assert float(np.max(np.abs(got - ref))) < 2e-6 * scale
