@@ -36,7 +36,7 @@ def test_headline_workload_full_size():
     src = FormTransportSource(L, q)
     src_o = o.form_source(q_cell=q)
     ndof = L.ndof
-    assert rel_err(src.reshape(nw, ndof)[pick], src_o.reshape(8, ndof)) < 1e-14
+    assert rel_err(src.reshape(nw, ndof)[pick], src_o.reshape(8, ndof)) < 1e-12
     ref = o.mult(src_o).reshape(8, ndof)
     d = torch.from_numpy(src).cuda()
     psi = torch.empty_like(d)
