@@ -55,6 +55,10 @@ int check_status(Handle& h) {
         CUDA_OR_FAIL(h, cudaMemsetAsync(h.d_status, 0, sizeof(int), h.stream));
         if (st & allium::kErrSingular) { h.last_error = "zero pivot in a local solve"; return ALLIUM_ERR_SINGULAR; }
         if (st & allium::kErrTimeout) { h.last_error = "a bounded device wait gave up"; return ALLIUM_ERR_TIMEOUT; }
+        if (st & allium::kErrSchedule) {
+            h.last_error = "a warp of the fused schedule holds more cells than its table slots";
+            return ALLIUM_ERR_UNSUPPORTED;
+        }
         if (st & allium::kErrFixup) {
             h.last_error = "Ryosuke fixup with more than three positive entries (src/fixup.cpp:155 aborts)";
             return ALLIUM_ERR_UNSUPPORTED;

@@ -23,17 +23,22 @@
 //
 // k_fused_level work unit: one thread per (cell, angle, group) node of a level.
 // Nodes come from a record {cell, angle | face pattern << 16}, sorted within
-// each level by (cell, face pattern, angle).  Each warp copies the FP32 tables
-// of its cells (G_d, M, [Mt], F_k and the outward face normals, 1.5 KB for a
-// trilinear hex) into shared memory with cp.async.bulk and an mbarrier per copy
-// (four cells per round), while its lanes load their upwind traces (one 32-byte
-// neighbour block when the face's DOF map is the standard one).  Each row of
-// the local system is then assembled from shared memory with packed FP32
-// (f32x2) FMAs and eliminated against the rows above, so that only the upper
-// triangle stays in registers.  Consecutive level launches overlap through
-// programmatic dependent launch: a level's blocks load their records, tables
-// and sources while the previous level drains, and wait before reading
-// upwind traces.
+// each level by (cell, face pattern, angle) and packed so that a warp holds at
+// most kSlots cells (padding records {-1, 0} close a warp early).  Each warp
+// copies the FP32 tables of its cells (G_d, M, [Mt], F_k and the outward face
+// normals, 1.5 KB for a trilinear hex) into shared memory with cp.async.bulk
+// and an mbarrier per copy, one slot per cell, while its lanes load their
+// sources and, after griddepcontrol.wait, their upwind traces (one 32-byte
+// neighbour block per inflow face when the face's DOF map is the standard
+// one), folded into the right-hand side as they arrive.  Each row of the local
+// system is then assembled from shared memory with packed FP32 (f32x2) FMAs,
+// eliminated against the rows above and scaled by its pivot's reciprocal, so
+// that only the strict upper triangle of a unit-diagonal U stays in registers.
+// Consecutive level launches overlap through programmatic dependent launch: a
+// level's blocks load their records, tables and sources while the previous
+// level drains.  (Factoring before the wait, to overlap the elimination with
+// the previous level as well, measured slower: the factors held across the
+// wait spill.)
 //
 // Layout of every psi-sized vector here (the "fused layout"):
 //     v[((g * Ne + e) * Nw + a) * n + i],
@@ -100,6 +105,11 @@ struct DTab {
 
 constexpr int kFusedBlock = 128;
 constexpr int kFusedWarps = kFusedBlock / 32;
+// the sweep's level kernel: 64-thread blocks, at most 96 registers (10 blocks
+// per SM); smaller blocks finish a level's last wave sooner
+constexpr int kSweepBlock = 64;
+constexpr int kSweepWarps = kSweepBlock / 32;
+constexpr int kSweepMinBlocks = 10;
 constexpr int kSlots = 4;          // staged cell tables per warp and round (sweep)
 constexpr int kSlotsDF = 2;        // staged cell tables per warp and round (residual)
 constexpr int kWaitLimit = 1 << 20;
@@ -236,6 +246,10 @@ __device__ __forceinline__ float get(const float2 (&row)[NP], int j) {
 template <int NP>
 __device__ __forceinline__ void fma_to(float2 (&row)[NP], int j, float a, float b) {
     if (j & 1) row[j >> 1].y = fmaf(a, b, row[j >> 1].y); else row[j >> 1].x = fmaf(a, b, row[j >> 1].x);
+}
+template <int NP>
+__device__ __forceinline__ void put(float2 (&row)[NP], int j, float v) {
+    if (j & 1) row[j >> 1].y = v; else row[j >> 1].x = v;
 }
 
 template <int N>
@@ -595,6 +609,45 @@ __global__ void k_unit_kahn(int Nw, int dim, const int* __restrict__ key, const 
     }
 }
 
+// Packs one level's records (sorted by cell) into warps of 32 lanes that hold at
+// most kSlots cells each: a cell's run of records that would be the warp's
+// kSlots+1-th starts the next warp instead, and the level is padded to whole
+// warps, padding records {-1, 0}.  One thread per level, sequential over the
+// level's records.  With out == nullptr only the padded sizes are written.
+__global__ void k_pack_levels(int nlev, const long long* __restrict__ starts, const int2* __restrict__ recs,
+                              const long long* __restrict__ out_starts, int2* __restrict__ out,
+                              long long* __restrict__ sizes) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nlev) return;
+    const long long s = starts[l], end = starts[l + 1];
+    int2* o = out ? out + out_starts[l] : nullptr;
+    long long pos = 0;
+    int runs = 0;   // cells touching the warp that holds lane pos
+    for (long long i = s; i < end;) {
+        const int c = recs[i].x;
+        long long j = i + 1;
+        while (j < end && recs[j].x == c) ++j;
+        const long long len = j - i;
+        if ((pos & 31) == 0) runs = 0;
+        if (runs == kSlots) {
+            const long long np = (pos + 31) & ~31LL;
+            if (o)
+                for (long long q = pos; q < np; ++q) o[q] = make_int2(-1, 0);
+            pos = np;
+            runs = 0;
+        }
+        if (o)
+            for (long long q = 0; q < len; ++q) o[pos + q] = recs[i + q];
+        runs = ((pos + len - 1) >> 5) == (pos >> 5) ? runs + 1 : 1;
+        pos += len;
+        i = j;
+    }
+    const long long np = (pos + 31) & ~31LL;
+    if (o)
+        for (long long q = pos; q < np; ++q) o[q] = make_int2(-1, 0);
+    if (sizes) sizes[l] = np;
+}
+
 __global__ void k_fused_cells(int ne, int dim, int p, int nf, const Slot* __restrict__ slots,
                               const uint8_t* __restrict__ nbrmap, int* __restrict__ nbr, unsigned* __restrict__ map) {
     const int nface = 2 * dim;
@@ -737,24 +790,25 @@ struct FusedArgs {
 };
 
 template <int D, int P, bool TD>
-__global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int base, int count) {
+__global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(FusedArgs f, int base, int count) {
     using S = Shape<D, P>;
     using T = Tab<D, P, TD>;
     constexpr int N = S::N, NF = S::NF, NFACE = S::NFACE;
     constexpr int NP = (N + 1) / 2;
-    __shared__ __align__(128) float s_tab[kFusedWarps * kSlots * T::size];
-    __shared__ __align__(8) unsigned long long s_bar[kFusedWarps * kSlots];
+    __shared__ __align__(128) float s_tab[kSweepWarps * kSlots * T::size];
+    __shared__ __align__(8) unsigned long long s_bar[kSweepWarps * kSlots];
     griddep_launch_dependents();
     const int warp = threadIdx.x >> 5;
     const long long total = (long long)count * f.G;
-    const long long t = (long long)blockIdx.x * kFusedBlock + threadIdx.x;
-    const bool valid = t < total;
+    const long long t = (long long)blockIdx.x * kSweepBlock + threadIdx.x;
+    bool valid = false;
     int g = 0, e = 0, a = 0, pat = 0;
-    if (valid) {
+    if (t < total) {
         g = (int)(t / count);
         const int ni = (int)(t - (long long)g * count);
         const int2 r = f.nodes[base + ni];
-        e = r.x;
+        valid = r.x >= 0;            // padding records close a warp early
+        e = valid ? r.x : 0;
         a = r.y & 0xffff;
         pat = (int)((unsigned)r.y >> 16);
     }
@@ -834,7 +888,13 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
         });
     }
 
-    for_each_round<kSlots>(wtab, wbar, f.tab, T::size, valid, run, start, e, f.status, [&](unsigned tb) {
+    // the schedule packs at most kSlots cells into a warp, so every table of the
+    // warp was staged by stage_runs
+    const bool staged = valid && run < kSlots;
+    if (valid && !staged) atomicOr(f.status, kErrSchedule);
+    if (staged) {
+        wait_copy(&wbar[run], 0u, f.status);
+        const unsigned tb = smem_u32(wtab + run * T::size);
         const float omv[3] = {om.x, om.y, om.z};
         // |Omega.n| on the outflow faces
         float dk[NFACE];
@@ -850,10 +910,10 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
             }
         }
         // rows of A = sum_d Omega_d G_d + sigma M [+ tau Mt] + sum_{outflow} |Omega.n| F_k,
-        // assembled one at a time and eliminated against the rows above (no pivoting);
-        // only the upper triangle U and the reciprocal pivots stay live
+        // assembled one at a time, eliminated against the rows above (no pivoting)
+        // and scaled by their pivot's reciprocal: only the strict upper triangle of
+        // the unit-diagonal U (and the scaled right-hand side) stays live
         float2 U[N][NP] = {};
-        float rinv[N] = {};
         bool ok = true;
         sfor<0, N>([&](auto ic) {
             constexpr int i = decltype(ic)::value;
@@ -892,21 +952,21 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
             float y = b[i];
             sfor<0, i>([&](auto mc) {
                 constexpr int m = decltype(mc)::value;
-                const float l = get(ar, m) * rinv[m];
+                const float l = get(ar, m);
                 sfor<(m + 1) / 2, NP>([&](auto pc) {
                     constexpr int p = decltype(pc)::value;
                     ar[p] = fma2(f2(-l), U[m][p], ar[p]);
                 });
                 y = fmaf(-l, b[m], y);
             });
-            b[i] = y;
-            sfor<i / 2, NP>([&](auto pc) {
-                constexpr int p = decltype(pc)::value;
-                U[i][p] = ar[p];
-            });
             const float piv = get(ar, i);
             ok = ok && (piv != 0.f);
-            rinv[i] = rcp_approx(piv);
+            const float r = rcp_approx(piv);
+            b[i] = y * r;
+            sfor<(i + 1) / 2, NP>([&](auto pc) {
+                constexpr int p = decltype(pc)::value;
+                U[i][p] = mul2(f2(r), ar[p]);
+            });
         });
         float x[N] = {};
         sfor<0, N>([&](auto kc) {
@@ -916,7 +976,7 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
                 constexpr int j = decltype(jc)::value;
                 v = fmaf(-get(U[k], j), x[j], v);
             });
-            x[k] = v * rinv[k];
+            x[k] = v;
         });
         if (!ok) atomicOr(f.status, kErrSingular);
         st_vec<N>(f.psi + idx, x);
@@ -936,7 +996,7 @@ __global__ void __launch_bounds__(kFusedBlock, 5) k_fused_level(FusedArgs f, int
             st_vec<N>(f.acc_hi + idx, h);
             st_vec<N>(f.acc_lo + idx, l);
         }
-    });
+    }
 }
 
 // ---------------------------------------------------------------- moments
@@ -1494,7 +1554,12 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     const int end_bit = 36 + lev_bits;
     std::vector<long long> hs(nlev + 1);
     auto step = [&](cudaError_t e) { if (err == cudaSuccess) err = e; };
-    step(cudaMalloc(&fs.nodes, N * sizeof(int2)));
+    int2* sorted = nullptr;
+    long long *psize = nullptr, *pstart = nullptr;
+    std::vector<long long> ps(nlev + 1, 0);
+    step(cudaMalloc(&sorted, N * sizeof(int2)));
+    step(cudaMalloc(&psize, (nlev + 1) * sizeof(long long)));
+    step(cudaMalloc(&pstart, (nlev + 1) * sizeof(long long)));
     step(cudaMalloc(&fs.nbr, (size_t)h.ne * h.nface * sizeof(int)));
     step(cudaMalloc(&fs.map, (size_t)h.ne * h.nface * sizeof(unsigned)));
     step(cudaMalloc(&fs.omega, (size_t)h.Nw * sizeof(float4)));
@@ -1512,20 +1577,38 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
         step(cudaGetLastError());
     }
     if (err == cudaSuccess)
-        step(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys_out, recs, fs.nodes, (int)N, 0, end_bit,
+        step(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys_out, recs, sorted, (int)N, 0, end_bit,
                                              h.stream));
     if (err == cudaSuccess) step(cudaMalloc(&tmp, tmp_bytes));
     if (err == cudaSuccess)
-        step(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_out, recs, fs.nodes, (int)N, 0, end_bit,
+        step(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_out, recs, sorted, (int)N, 0, end_bit,
                                              h.stream));
     if (err == cudaSuccess) {
         k_level_starts<<<blocks(nlev + 1, 128), 128, 0, h.stream>>>(nlev, keys_out, N, starts);
         step(cudaGetLastError());
     }
+    // warps of at most kSlots cells: padded level sizes, their offsets, then the records
+    if (err == cudaSuccess) {
+        k_pack_levels<<<blocks(nlev, 64), 64, 0, h.stream>>>(nlev, starts, sorted, nullptr, nullptr, psize);
+        step(cudaGetLastError());
+    }
     if (err == cudaSuccess)
-        step(cudaMemcpyAsync(hs.data(), starts, (nlev + 1) * sizeof(long long), cudaMemcpyDeviceToHost, h.stream));
+        step(cudaMemcpyAsync(hs.data(), psize, nlev * sizeof(long long), cudaMemcpyDeviceToHost, h.stream));
+    if (err == cudaSuccess) step(cudaStreamSynchronize(h.stream));
+    if (err == cudaSuccess) {
+        for (int l = 0; l < nlev; ++l) ps[l + 1] = ps[l] + hs[l];
+        if (ps[nlev] > 0x7fffffffLL) err = cudaErrorInvalidValue;
+    }
+    if (err == cudaSuccess) step(cudaMalloc(&fs.nodes, (size_t)ps[nlev] * sizeof(int2)));
+    if (err == cudaSuccess)
+        step(cudaMemcpyAsync(pstart, ps.data(), (nlev + 1) * sizeof(long long), cudaMemcpyHostToDevice, h.stream));
+    if (err == cudaSuccess) {
+        k_pack_levels<<<blocks(nlev, 64), 64, 0, h.stream>>>(nlev, starts, sorted, pstart, fs.nodes, nullptr);
+        step(cudaGetLastError());
+    }
     if (err == cudaSuccess) step(cudaStreamSynchronize(h.stream));
     cudaFree(tmp); cudaFree(starts); cudaFree(keys_out); cudaFree(keys); cudaFree(recs);
+    cudaFree(sorted); cudaFree(psize); cudaFree(pstart);
     cudaFree(unit); cudaFree(ulevel);
     if (err == cudaSuccess) {
         k_fused_cells<<<blocks((long long)h.ne * h.nface, 256), 256, 0, h.stream>>>(h.ne, h.dim, h.p, h.nf, h.d_slots,
@@ -1544,7 +1627,7 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     }
     fs.num_levels = nlev;
     fs.level_offsets.assign(nlev + 1, 0);
-    for (int l = 0; l <= nlev; ++l) fs.level_offsets[l] = (int)hs[l];
+    for (int l = 0; l <= nlev; ++l) fs.level_offsets[l] = (int)ps[l];
     return cudaSuccess;
 }
 
@@ -1566,8 +1649,8 @@ cudaError_t sweep_body(Handle& h, FusedState& fs, const FusedArgs& a, double* ph
         if (count == 0) continue;
         const long long threads = (long long)count * h.G;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(blocks(threads, kFusedBlock));
-        cfg.blockDim = dim3(kFusedBlock);
+        cfg.gridDim = dim3(blocks(threads, kSweepBlock));
+        cfg.blockDim = dim3(kSweepBlock);
         cfg.stream = st;
         // every level after the first may start its blocks while the previous
         // level drains; they wait (griddepcontrol.wait) before reading upwind traces

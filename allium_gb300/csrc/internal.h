@@ -211,6 +211,7 @@ constexpr int kErrSingular = 1;
 constexpr int kErrNaN = 2;
 constexpr int kErrTimeout = 4;
 constexpr int kErrFixup = 8;     // Ryosuke fixup with more than three positive entries
+constexpr int kErrSchedule = 16; // a fused-sweep warp holds more cells than its table slots
 // node-groups per tile of the dataflow schedule (= threads per block)
 constexpr int kTile = 128;
 

@@ -13,9 +13,14 @@ sum; scaling sigma_s by (slice weight sum / full weight sum) makes it divide by
 the full sum, as the unsharded D^T does (src/transport_op.cpp:33-89).
 
 Ranks talk through torch.distributed (NCCL between GPUs; gloo for the CPU
-tests).  The sweep side is a backend object with source(q_cell),
+tests and for ranks that share one GPU, where the moments pass through host
+memory).  The sweep side is a backend object with source(q_cell),
 scatter(sigma_s, phi, q), mult(psi) and moments(psi); GPUBackend wraps the
 library's handle.
+
+AngleShardedSI is source iteration; AngleShardedGMRES is GMRES on the
+scalar-flux system T phi = b (the Krylov option of exe/chive.cpp:704-735) with
+the same single exchange per application of T.
 """
 from __future__ import annotations
 
@@ -64,6 +69,20 @@ class GPUBackend:
         out = torch.empty(self.phi_size, dtype=torch.float64, device=psi.device)
         self.D.Mult(psi, out)
         return out
+
+
+def allreduce_sum(t, group=None):
+    """In-place sum of t over the ranks of group.  gloo reduces host tensors:
+    a CUDA tensor goes through a host copy there (ranks that share one GPU, or
+    a CPU-only world)."""
+    import torch.distributed as dist
+    if t.is_cuda and dist.get_backend(group) == "gloo":
+        h = t.cpu()
+        dist.all_reduce(h, op=dist.ReduceOp.SUM, group=group)
+        t.copy_(h)
+    else:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return t
 
 
 class AngleShardedSI:
@@ -119,7 +138,7 @@ class AngleShardedSI:
             psi = self.b.scatter(self.sigma_s, zero, q)
             psi = self.b.mult(psi)
             new = self.b.moments(psi)
-            dist.all_reduce(new, op=dist.ReduceOp.SUM, group=self.group)   # the one exchange
+            allreduce_sum(new, self.group)   # the one exchange
             it += 1
             if self.ng == 1:
                 change = (torch.linalg.norm(new - zero) / torch.linalg.norm(new)).item()
@@ -127,9 +146,50 @@ class AngleShardedSI:
                 # every rank of a group slice holds the same moments: the world sums
                 # count each slice na times, which cancels in the ratio
                 sq = torch.stack([torch.sum((new - zero) ** 2), torch.sum(new * new)])
-                dist.all_reduce(sq, op=dist.ReduceOp.SUM, group=self.world_group)
+                allreduce_sum(sq, self.world_group)
                 change = float(torch.sqrt(sq[0] / sq[1]).item())
             phi = new
             if change < tol:
                 break
         return phi, it, change < tol
+
+
+class AngleShardedGMRES(AngleShardedSI):
+    """GMRES on T phi = (I - D L^{-1} D^T S) phi = D L^{-1} q = b with the
+    directions (and optionally the groups) split over the ranks.
+
+    T x = x - sum_r D_r L_r^{-1} D_r^T S x: each rank sweeps its slice and one
+    allreduce of the moments over the direction slices of its group slice
+    completes the product, as in source iteration.  After that exchange every
+    rank of a group slice holds the same Krylov vectors (the group slice's part
+    of phi), so inner products need a second reduction only across group
+    slices: reduce() sums the partial dot products over the world and divides
+    by the number of ranks holding each slice.  With group_shards = 1 every
+    rank repeats the same small Hessenberg work and no dot product is
+    exchanged."""
+
+    def _reduce(self, t):
+        allreduce_sum(t, self.world_group)
+        t /= self.na
+        return t
+
+    def apply(self, x, out):
+        psi = self.b.scatter(self.sigma_s, x, None)
+        psi = self.b.mult(psi)
+        part = self.b.moments(psi)
+        allreduce_sum(part, self.group)
+        torch.sub(x, part, out=out)
+        self.sweeps += 1
+        return out
+
+    def solve(self, q_cell, tol=1e-8, restart=30, maxiter=1000):
+        """Returns (phi of this rank's groups [g1 - g0] x Ndof, iterations, converged)."""
+        from .solvers import gmres
+        q_cell = np.ascontiguousarray(q_cell, dtype=np.float64)[self.g0:self.g1]
+        self.q = self.b.source(q_cell)
+        self.sweeps = 0
+        b = self.b.moments(self.b.mult(self.q.clone()))
+        allreduce_sum(b, self.group)
+        phi, it, hist = gmres(self.apply, b, tol=tol, restart=restart, maxiter=maxiter,
+                              reduce=self._reduce if self.ng > 1 else None)
+        return phi, it, hist[-1] <= tol

@@ -137,7 +137,8 @@ def source_iteration(op: SchurOperator, q, tol=1e-8, maxiter=10000, phi0=None, d
     return SolveResult(phi, it, conv, hist, time.perf_counter() - t0, op.sweeps64, op.sweeps32)
 
 
-def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=None, final_residual=True):
+def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=None, final_residual=True,
+          reduce=None):
     """Restarted GMRES on torch vectors; stops when ||b - A x|| <= max(tol ||b||, atol)
     (the Arnoldi residual estimate).  prec(v, out) is a right preconditioner,
     kept in flexible form (the preconditioned directions are stored), so it
@@ -145,10 +146,27 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=
     iterate is recomputed with one more application of A after each cycle
     (restart or stop); without it the last cycle that meets the tolerance ends on
     the Arnoldi estimate (for inner solves whose caller checks the residual
-    itself).  Returns (x, iterations, history)."""
+    itself).  reduce(t), when given, sums a tensor of partial inner products
+    over the shards of a distributed vector in place (every vector here is then
+    one shard); the Hessenberg work is repeated identically on every shard.
+    Returns (x, iterations, history)."""
     dev, n = b.device, b.numel()
     x = torch.zeros_like(b) if x0 is None else x0.clone()
-    bnorm = torch.linalg.norm(b).item()
+
+    def norm(v):
+        if reduce is None:
+            return torch.linalg.norm(v).item()
+        s = torch.dot(v, v).reshape(1)
+        reduce(s)
+        return math.sqrt(max(s.item(), 0.0))
+
+    def dots(Vk, v):
+        h = torch.mv(Vk, v)
+        if reduce is not None:
+            reduce(h)
+        return h
+
+    bnorm = norm(b)
     if bnorm == 0.0:
         return x, 0, [0.0]
     target = max(tol * bnorm, atol)
@@ -161,7 +179,7 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=
     if x0 is not None:
         apply(x, w)
         r = b - w
-    beta = torch.linalg.norm(r).item()
+    beta = norm(r)
     hist.append(beta / bnorm)
     while it < maxiter and beta > target:
         V[0] = r / beta
@@ -178,12 +196,12 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=
                 apply(V[k], w)
             it += 1
             # classical Gram-Schmidt, twice
-            h = torch.mv(V[: k + 1], w)
+            h = dots(V[: k + 1], w)
             w -= torch.mv(V[: k + 1].t(), h)
-            h2 = torch.mv(V[: k + 1], w)
+            h2 = dots(V[: k + 1], w)
             w -= torch.mv(V[: k + 1].t(), h2)
             hk = (h + h2).cpu().numpy()
-            hn = torch.linalg.norm(w).item()
+            hn = norm(w)
             H[: k + 1, k] = hk
             H[k + 1, k] = hn
             for i in range(k):
@@ -209,7 +227,7 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=
             break
         apply(x, w)
         r = b - w
-        beta = torch.linalg.norm(r).item()
+        beta = norm(r)
         hist[-1] = beta / bnorm
     return x, it, hist
 

@@ -455,6 +455,35 @@ def batch_section(count):
     return out
 
 
+def sharded_section(mesh, quad, sigma, q, rank, world, barrier, max_over_ranks):
+    """The C2 solve with the directions split over the ranks (run under
+    torchrun, N > 1): AngleShardedGMRES to 1e-8, each rank a handle over its
+    slice of the S12 directions, one NCCL allreduce of the FP64 moments per
+    application of T.  Strong scaling of one problem, reported beside the
+    weak-scaled headline."""
+    import torch
+    from allium_gb300.sharded import AngleShardedGMRES
+    rng = np.random.default_rng(SEED + 2)
+    sigma_s = sigma * rng.uniform(0.5, 0.999, size=sigma.shape)
+    t0 = time.perf_counter()
+    solver = AngleShardedGMRES(mesh, ORDER, quad, sigma, sigma_s, rank, world)
+    barrier()
+    setup_s = max_over_ranks(time.perf_counter() - t0)
+    solver.solve(q, tol=1e-8)        # warm-up: factor pass of each slice handle, graphs
+    barrier()
+    t0 = time.perf_counter()
+    phi, it, conv = solver.solve(q, tol=1e-8)
+    torch.cuda.synchronize()
+    seconds = max_over_ranks(time.perf_counter() - t0)
+    out = {"seconds": seconds, "setup_seconds": setup_s, "iterations": it, "converged": bool(conv),
+           "directions_per_rank": solver.a1 - solver.a0, "ranks": world,
+           "exchange": "one NCCL allreduce of G*Ndof FP64 moments per application of T",
+           "scaling": "strong (one problem split by direction)"}
+    del solver
+    torch.cuda.empty_cache()
+    return out
+
+
 def warm_solver_libraries():
     """Untimed: one pass of every solver path on a 24x24 problem and a few
     training steps of the cell network.  On a fresh
@@ -710,6 +739,10 @@ def run_gpu(args):
     L.synchronize()
     assert torch.equal(h_psi, psi.cpu()), "host and device paths disagree"
 
+    sharded = None
+    if world > 1:
+        sharded = sharded_section(mesh, quad, sigma, q, rank, world, barrier, max_over_ranks)
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -784,6 +817,7 @@ def run_gpu(args):
                 "note": ("the inner operator phi = D L^-1 (D^T S x / sum w) of the refinement: per-cell source "
                          "in registers, FP32 local solves, moments in double-float; 8 B per entry is the "
                          "FP32 sweep's algorithmic traffic (read q, write psi)")},
+            "sharded_c2": sharded,
             "double_float_residual_ms": ms_resid,
             "double_float_moments_ms": ms_mom_df,
             "clocks": clk.summary()}

@@ -1,6 +1,7 @@
-"""The angle-sharded source iteration on two and three CPU ranks (gloo): each
-rank sweeps its slice of the directions with the oracle standing in for its
-GPU, one allreduce of the moments per iteration; the result equals the
+"""The angle-sharded source iteration and GMRES on two to four CPU ranks
+(gloo): each rank sweeps its slice of the directions with the oracle standing
+in for its GPU, one allreduce of the moments per application of the operator
+(and, with group slices, of the Krylov inner products); the result equals the
 unsharded iteration to 1e-10 relative."""
 import os
 import socket
@@ -22,7 +23,8 @@ class OracleBackend:
         return torch.from_numpy(self.o.form_source(q_cell=q_cell))
 
     def scatter(self, sigma_s, phi, q):
-        return torch.from_numpy(self.o.scattering_source(sigma_s, phi.numpy(), q.numpy()))
+        qn = np.zeros(self.o.G * self.o.Nw * self.o.ndof) if q is None else q.numpy()
+        return torch.from_numpy(self.o.scattering_source(sigma_s, phi.numpy(), qn))
 
     def mult(self, psi):
         return torch.from_numpy(self.o.mult(psi.numpy()))
@@ -36,14 +38,15 @@ def _case():
     return mesh, quad, sigma, 0.8 * sigma, np.ones((2, mesh.num_elements))
 
 
-def _worker(rank, world, port, path, group_shards=1):
+def _worker(rank, world, port, path, group_shards=1, method="si"):
     import torch.distributed as dist
-    from allium_gb300.sharded import AngleShardedSI
+    from allium_gb300.sharded import AngleShardedGMRES, AngleShardedSI
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     mesh, quad, sigma, ss, q = _case()
-    solver = AngleShardedSI(mesh, 1, quad, sigma, ss, rank, world, backend=OracleBackend, group_shards=group_shards)
+    cls = AngleShardedSI if method == "si" else AngleShardedGMRES
+    solver = cls(mesh, 1, quad, sigma, ss, rank, world, backend=OracleBackend, group_shards=group_shards)
     phi, it, conv = solver.solve(q, tol=1e-12, maxiter=500)
     np.save(f"{path}.{rank}.npy", np.concatenate([phi.numpy(), [solver.g0, solver.g1, it, conv]]))
     dist.destroy_process_group()
@@ -113,3 +116,39 @@ def test_angle_sharded_si(tmp_path, world):
             break
     assert it == int(r0[-2])
     assert np.max(np.abs(r0[:-2] - phi)) < 1e-10 * np.max(np.abs(phi))
+
+
+def _unsharded_gmres():
+    from allium_gb300.solvers import gmres
+    from oracle.oracle import OracleSweep
+    mesh, quad, sigma, ss, q = _case()
+    o = OracleSweep(mesh, 1, quad, sigma)
+    src = o.form_source(q_cell=q)
+    zero = np.zeros(src.size)
+    b = torch.from_numpy(o.moments(o.mult(src)))
+
+    def apply(x, out):
+        out.copy_(x - torch.from_numpy(o.moments(o.mult(o.scattering_source(ss, x.numpy(), zero)))))
+        return out
+
+    phi, it, hist = gmres(apply, b, tol=1e-12, restart=30, maxiter=500)
+    return phi.numpy().reshape(o.G, -1), it
+
+
+@pytest.mark.parametrize("world,group_shards", [(2, 1), (3, 1), (4, 2)])
+def test_angle_sharded_gmres(tmp_path, world, group_shards):
+    # direction slices (one Krylov space repeated on every rank) and a 2 x 2
+    # grid whose Krylov vectors are split by group (inner products reduced)
+    mp = pytest.importorskip("torch.multiprocessing")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    path = str(tmp_path / "phi")
+    mp.spawn(_worker, args=(world, port, path, group_shards, "gmres"), nprocs=world, join=True)
+    ref, it_ref = _unsharded_gmres()
+    for r in range(world):
+        res = np.load(f"{path}.{r}.npy")
+        g0, g1, it, conv = int(res[-4]), int(res[-3]), int(res[-2]), res[-1]
+        assert conv == 1.0 and it == it_ref
+        got = res[:-4].reshape(g1 - g0, -1)
+        assert np.max(np.abs(got - ref[g0:g1])) < 1e-10 * np.max(np.abs(ref))
