@@ -111,6 +111,12 @@ EXPORTS = {
     "allium_mlp_adam": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                                   C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]),
     "allium_mlp_to_bf16": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "allium_mlp_gemm_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong,
+                                     C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong, C.c_void_p, C.c_float,
+                                     C.c_float, C.c_int, C.c_int, C.c_void_p]),
+    "allium_mlp_transpose_bf16": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong,
+                                            C.c_void_p]),
+    "allium_mlp_status": (C.c_int, [C.c_void_p]),
     "allium_fp64_fma_probe": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_void_p, C.c_void_p]),
     "allium_sweep_synchronize": (C.c_int, [C.c_void_p]),
     "allium_sweep_last_error": (C.c_char_p, [C.c_void_p]),

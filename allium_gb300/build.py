@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liballium_sweep.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["api.cu", "setup.cu", "sweep_fp64.cu", "sweep_fp32.cu", "topology.cpp", "balance_noalloc.cu", "fused.cu", "peak.cu", "trt.cu", "dsa.cu", "mlp.cu"]
+SOURCES = ["api.cu", "setup.cu", "sweep_fp64.cu", "sweep_fp32.cu", "topology.cpp", "balance_noalloc.cu", "fused.cu", "peak.cu", "trt.cu", "dsa.cu", "mlp.cu", "mlp_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", CSRC, "-I", INCLUDE]

@@ -609,43 +609,69 @@ __global__ void k_unit_kahn(int Nw, int dim, const int* __restrict__ key, const 
     }
 }
 
-// Packs one level's records (sorted by cell) into warps of 32 lanes that hold at
-// most kSlots cells each: a cell's run of records that would be the warp's
-// kSlots+1-th starts the next warp instead, and the level is padded to whole
-// warps, padding records {-1, 0}.  One thread per level, sequential over the
-// level's records.  With out == nullptr only the padded sizes are written.
-__global__ void k_pack_levels(int nlev, const long long* __restrict__ starts, const int2* __restrict__ recs,
-                              const long long* __restrict__ out_starts, int2* __restrict__ out,
-                              long long* __restrict__ sizes) {
+// Packing of a level's records into warps of 32 lanes that hold at most
+// kSlots cells each: a cell's run of records that would be a warp's
+// kSlots+1-th cell starts the next warp instead, and each level is padded to
+// whole warps with records {-1, 0}.  Runs (records of one cell within one
+// level, consecutive after the sort) are found in parallel; the greedy
+// placement walks a level's runs in one thread; the records are then scattered
+// in parallel.
+__global__ void k_run_flags(long long n, const unsigned long long* __restrict__ keys, const int2* __restrict__ recs,
+                            int* __restrict__ flag) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (i == 0 || (keys[i] >> 36) != (keys[i - 1] >> 36) || recs[i].x != recs[i - 1].x) ? 1 : 0;
+}
+
+// run_start[r] = first record of run r (flag[i] == 1, ridx[i] its exclusive scan)
+__global__ void k_run_starts(long long n, const int* __restrict__ flag, const int* __restrict__ ridx,
+                             int* __restrict__ run_start) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) run_start[ridx[i]] = (int)i;
+}
+
+// one thread per level: padded position of each of its runs, padded level size
+__global__ void k_pack_runs(int nlev, long long n, int nruns, const long long* __restrict__ starts,
+                            const int* __restrict__ ridx, const int* __restrict__ run_start, int* __restrict__ run_pos,
+                            long long* __restrict__ sizes) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= nlev) return;
-    const long long s = starts[l], end = starts[l + 1];
-    int2* o = out ? out + out_starts[l] : nullptr;
-    long long pos = 0;
-    int runs = 0;   // cells touching the warp that holds lane pos
-    for (long long i = s; i < end;) {
-        const int c = recs[i].x;
-        long long j = i + 1;
-        while (j < end && recs[j].x == c) ++j;
-        const long long len = j - i;
-        if ((pos & 31) == 0) runs = 0;
-        if (runs == kSlots) {
-            const long long np = (pos + 31) & ~31LL;
-            if (o)
-                for (long long q = pos; q < np; ++q) o[q] = make_int2(-1, 0);
-            pos = np;
-            runs = 0;
-        }
-        if (o)
-            for (long long q = 0; q < len; ++q) o[pos + q] = recs[i + q];
-        runs = ((pos + len - 1) >> 5) == (pos >> 5) ? runs + 1 : 1;
-        pos += len;
-        i = j;
+    if (starts[l] == starts[l + 1]) {
+        sizes[l] = 0;
+        return;
     }
-    const long long np = (pos + 31) & ~31LL;
-    if (o)
-        for (long long q = pos; q < np; ++q) o[q] = make_int2(-1, 0);
-    if (sizes) sizes[l] = np;
+    const int r0 = ridx[starts[l]];
+    const int r1 = starts[l + 1] < n ? ridx[starts[l + 1]] : nruns;
+    long long pos = 0;
+    int cells = 0;   // cells touching the warp that holds lane pos
+    for (int r = r0; r < r1; ++r) {
+        const long long len = (long long)(r + 1 < nruns ? run_start[r + 1] : n) - run_start[r];
+        if ((pos & 31) == 0) cells = 0;
+        if (cells == kSlots) {
+            pos = (pos + 31) & ~31LL;
+            cells = 0;
+        }
+        run_pos[r] = (int)pos;
+        cells = ((pos + len - 1) >> 5) == (pos >> 5) ? cells + 1 : 1;
+        pos += len;
+    }
+    sizes[l] = (pos + 31) & ~31LL;
+}
+
+__global__ void k_pack_fill(long long n, int2* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_int2(-1, 0);
+}
+
+__global__ void k_pack_scatter(long long n, const unsigned long long* __restrict__ keys, const int2* __restrict__ recs,
+                               const int* __restrict__ ridx, const int* __restrict__ flag,
+                               const int* __restrict__ run_start, const int* __restrict__ run_pos,
+                               const long long* __restrict__ out_starts, int2* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = ridx[i] + flag[i] - 1;   // run of record i (inclusive scan - 1)
+    const int l = (int)(keys[i] >> 36);
+    out[out_starts[l] + run_pos[r] + (i - run_start[r])] = recs[i];
 }
 
 __global__ void k_fused_cells(int ne, int dim, int p, int nf, const Slot* __restrict__ slots,
@@ -1556,10 +1582,16 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     auto step = [&](cudaError_t e) { if (err == cudaSuccess) err = e; };
     int2* sorted = nullptr;
     long long *psize = nullptr, *pstart = nullptr;
+    int *flag = nullptr, *ridx = nullptr, *run_start = nullptr, *run_pos = nullptr;
+    void* scan_tmp = nullptr;
+    size_t scan_bytes = 0;
+    int nruns = 0;
     std::vector<long long> ps(nlev + 1, 0);
     step(cudaMalloc(&sorted, N * sizeof(int2)));
     step(cudaMalloc(&psize, (nlev + 1) * sizeof(long long)));
     step(cudaMalloc(&pstart, (nlev + 1) * sizeof(long long)));
+    step(cudaMalloc(&flag, N * sizeof(int)));
+    step(cudaMalloc(&ridx, N * sizeof(int)));
     step(cudaMalloc(&fs.nbr, (size_t)h.ne * h.nface * sizeof(int)));
     step(cudaMalloc(&fs.map, (size_t)h.ne * h.nface * sizeof(unsigned)));
     step(cudaMalloc(&fs.omega, (size_t)h.Nw * sizeof(float4)));
@@ -1587,9 +1619,26 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
         k_level_starts<<<blocks(nlev + 1, 128), 128, 0, h.stream>>>(nlev, keys_out, N, starts);
         step(cudaGetLastError());
     }
-    // warps of at most kSlots cells: padded level sizes, their offsets, then the records
+    // warps of at most kSlots cells: runs, their padded positions, level sizes, records
     if (err == cudaSuccess) {
-        k_pack_levels<<<blocks(nlev, 64), 64, 0, h.stream>>>(nlev, starts, sorted, nullptr, nullptr, psize);
+        k_run_flags<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, sorted, flag);
+        step(cudaGetLastError());
+    }
+    if (err == cudaSuccess) step(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, flag, ridx, (int)N, h.stream));
+    if (err == cudaSuccess) step(cudaMalloc(&scan_tmp, scan_bytes));
+    if (err == cudaSuccess) step(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, flag, ridx, (int)N, h.stream));
+    if (err == cudaSuccess) {
+        int last[2] = {0, 0};
+        step(cudaMemcpyAsync(&last[0], ridx + N - 1, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+        step(cudaMemcpyAsync(&last[1], flag + N - 1, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+        step(cudaStreamSynchronize(h.stream));
+        nruns = last[0] + last[1];
+    }
+    if (err == cudaSuccess) step(cudaMalloc(&run_start, (size_t)(nruns + 1) * sizeof(int)));
+    if (err == cudaSuccess) step(cudaMalloc(&run_pos, (size_t)(nruns + 1) * sizeof(int)));
+    if (err == cudaSuccess) {
+        k_run_starts<<<blocks(N, 256), 256, 0, h.stream>>>(N, flag, ridx, run_start);
+        k_pack_runs<<<blocks(nlev, 64), 64, 0, h.stream>>>(nlev, N, nruns, starts, ridx, run_start, run_pos, psize);
         step(cudaGetLastError());
     }
     if (err == cudaSuccess)
@@ -1603,12 +1652,15 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     if (err == cudaSuccess)
         step(cudaMemcpyAsync(pstart, ps.data(), (nlev + 1) * sizeof(long long), cudaMemcpyHostToDevice, h.stream));
     if (err == cudaSuccess) {
-        k_pack_levels<<<blocks(nlev, 64), 64, 0, h.stream>>>(nlev, starts, sorted, pstart, fs.nodes, nullptr);
+        k_pack_fill<<<blocks(ps[nlev], 256), 256, 0, h.stream>>>(ps[nlev], fs.nodes);
+        k_pack_scatter<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, sorted, ridx, flag, run_start, run_pos,
+                                                             pstart, fs.nodes);
         step(cudaGetLastError());
     }
     if (err == cudaSuccess) step(cudaStreamSynchronize(h.stream));
     cudaFree(tmp); cudaFree(starts); cudaFree(keys_out); cudaFree(keys); cudaFree(recs);
-    cudaFree(sorted); cudaFree(psize); cudaFree(pstart);
+    cudaFree(sorted); cudaFree(psize); cudaFree(pstart); cudaFree(flag); cudaFree(ridx); cudaFree(scan_tmp);
+    cudaFree(run_start); cudaFree(run_pos);
     cudaFree(unit); cudaFree(ulevel);
     if (err == cudaSuccess) {
         k_fused_cells<<<blocks((long long)h.ne * h.nface, 256), 256, 0, h.stream>>>(h.ne, h.dim, h.p, h.nf, h.d_slots,

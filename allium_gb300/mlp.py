@@ -1,6 +1,9 @@
 """A per-cell MLP trained and evaluated with the library's BF16 tensor-core
-kernels (allium_mlp_*: mma.sync GEMMs with FP32 accumulation, fused bias and
-ReLU, ReLU/bias/MSE gradients, Adam).
+kernels (allium_mlp_*: GEMMs with FP32 accumulation and a fused bias / ReLU
+epilogue on the fifth-generation tensor cores (tcgen05.mma, TMEM accumulators,
+operands by cp.async.bulk.tensor), ReLU/bias/MSE gradients, Adam).  The
+warp-level mma.sync GEMM stays available (gemm(..., tc=False)) as the
+comparison.
 
 CellMLP is layers x width (ReLU between layers, linear output), FP32 master
 weights W_l[K][N] with BF16 copies for the GEMMs.  LearnedInitialIterate wraps
@@ -42,11 +45,34 @@ def to_bf16(x):
     return y
 
 
-def gemm(A, B, out=None, out_bf16=None, bias=None, relu=False, alpha=1.0, beta=0.0, transA=False, transB=False):
-    """out[M][N] = alpha op(A) op(B) (+ beta out) (+ bias) (ReLU); A, B BF16 2-D tensors."""
+def _kmajor(X, trans):
+    """op(X) as a K-major BF16 matrix [R][Kp] with Kp a multiple of 8 (zero
+    columns beyond K), as the tensor-core GEMM's tensor maps need: X itself
+    when it already is one, else a copy (allium_mlp_transpose_bf16 when the
+    operand is stored transposed)."""
+    R, K = (X.shape[1], X.shape[0]) if trans else (X.shape[0], X.shape[1])
+    Kp = (K + 7) // 8 * 8
+    if not trans and Kp == K and X.stride(1) == 1 and X.stride(0) % 8 == 0 and X.data_ptr() % 16 == 0:
+        return X, X.stride(0)
+    out = (torch.zeros if Kp != K else torch.empty)((R, Kp), dtype=torch.bfloat16, device=X.device)
+    if trans:
+        assert X.stride(1) == 1
+        _ck(_lib.lib().allium_mlp_transpose_bf16(K, R, _p(X), X.stride(0), _p(out), Kp, _stream()))
+    else:
+        out[:, :K] = X
+    return out, Kp
+
+
+def gemm(A, B, out=None, out_bf16=None, bias=None, relu=False, alpha=1.0, beta=0.0, transA=False, transB=False,
+         tc=True):
+    """out[M][N] = alpha op(A) op(B) (+ beta out) (+ bias) (ReLU); A, B BF16 2-D tensors.
+    tc: the tcgen05 kernel (operands made K-major first where needed), else
+    the mma.sync kernel, which reads any strides."""
     M, K = (A.shape[1], A.shape[0]) if transA else (A.shape[0], A.shape[1])
     K2, N = (B.shape[1], B.shape[0]) if transB else (B.shape[0], B.shape[1])
     assert K == K2 and A.dtype == torch.bfloat16 and B.dtype == torch.bfloat16
+    if tc:
+        return gemm_tc(A, B, out, out_bf16, bias, relu, alpha, beta, transA, transB)
     sam, sak = (1, A.stride(0)) if transA else (A.stride(0), 1)
     sbk, sbn = (1, B.stride(0)) if transB else (B.stride(0), 1)
     assert A.stride(1) == 1 and B.stride(1) == 1
@@ -56,6 +82,35 @@ def gemm(A, B, out=None, out_bf16=None, bias=None, relu=False, alpha=1.0, beta=0
     _ck(_lib.lib().allium_mlp_gemm(M, N, K, _p(A), sam, sak, _p(B), sbk, sbn, _p(out), ldc, _p(out_bf16), _p(bias),
                                    float(alpha), float(beta), int(relu), _stream()))
     return out
+
+
+def gemm_tc(A, B, out=None, out_bf16=None, bias=None, relu=False, alpha=1.0, beta=0.0, transA=False, transB=False):
+    """gemm() on the tcgen05 kernel (allium_mlp_gemm_tc: C = A B^T with both
+    operands K-major).  Few output tiles over a long K (the weight gradients
+    over a batch) split K over blocks, partial sums added atomically."""
+    M, K = (A.shape[1], A.shape[0]) if transA else (A.shape[0], A.shape[1])
+    N = B.shape[0] if transB else B.shape[1]
+    a, lda = _kmajor(A, transA)
+    b, ldb = _kmajor(B, not transB)
+    if out is None and out_bf16 is None:
+        out = torch.empty((M, N), dtype=torch.float32, device=A.device)
+    bn = 256 if N > 128 else 128          # the kernel's tile width in N
+    tiles = ((M + 127) // 128) * ((N + bn - 1) // bn)
+    ksplit = 1
+    plain = out is not None and out_bf16 is None and bias is None and not relu and beta == 0.0
+    if plain and tiles < 152 and K >= 8 * 64:
+        ksplit = max(1, min((152 + tiles - 1) // tiles, K // (4 * 64)))
+    ldc = out.stride(0) if out is not None else 0
+    ldcb = out_bf16.stride(0) if out_bf16 is not None else 0
+    _ck(_lib.lib().allium_mlp_gemm_tc(M, N, K, _p(a), lda, _p(b), ldb, _p(out), ldc,
+                                      _p(out_bf16), ldcb, _p(bias), float(alpha), float(beta), int(relu), ksplit,
+                                      _stream()))
+    return out
+
+
+def tc_status():
+    """Raises if a bounded wait inside the tensor-core GEMM gave up (synchronizes)."""
+    _ck(_lib.lib().allium_mlp_status(_stream()))
 
 
 class CellMLP:

@@ -356,6 +356,60 @@ def trt_section(steps):
     return out
 
 
+def gemm_section(reps=20):
+    """The MLP's BF16 GEMMs on the tcgen05 kernel against the mma.sync kernel
+    (CUDA events, best of two rounds of `reps`): a hidden layer's forward
+    product over the wave's 16384 cells, its weight gradient (K = 16384, split
+    over blocks) and a 4096^3 product, where the tensor pipe rather than memory
+    bounds the kernel (its TFLOP/s against the measured cuBLAS BF16 rate)."""
+    import torch
+    from allium_gb300.mlp import gemm, tc_status
+    g = torch.Generator(device="cpu").manual_seed(5)
+    st = torch.cuda.current_stream()
+    out = {}
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        peak = 1900.0
+    cases = {"layer_forward": (16384, 256, 256, False, True),
+             "weight_gradient": (256, 256, 16384, True, False),
+             "square_4096": (4096, 4096, 4096, False, True)}
+    for name, (M, N, K, ta, tb) in cases.items():
+        A = torch.randn((K, M) if ta else (M, K), generator=g).to("cuda", torch.bfloat16)
+        B = torch.randn((N, K) if tb else (K, N), generator=g).to("cuda", torch.bfloat16)
+        C = torch.empty((M, N), dtype=torch.float32, device="cuda")
+        res = {"M": M, "N": N, "K": K}
+        for tc in (True, False):
+            fn = lambda: gemm(A, B, out=C, transA=ta, transB=tb, tc=tc)
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            best = float("inf")
+            for _ in range(2):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                for _ in range(reps):
+                    fn()
+                e1.record(st)
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1) / reps)
+            ref = C.clone() if tc else ref
+            res["tc_ms" if tc else "mma_sync_ms"] = best
+        tc_status()
+        res["rel_diff"] = float((torch.max(torch.abs(C - ref)) / torch.max(torch.abs(ref))).item())
+        res["tc_tflops"] = 2.0 * M * N * K / (res["tc_ms"] * 1e-3) / 1e12
+        res["mma_sync_tflops"] = 2.0 * M * N * K / (res["mma_sync_ms"] * 1e-3) / 1e12
+        res["tc_frac_of_measured_bf16"] = res["tc_tflops"] / peak
+        out[name] = res
+        del A, B, C, ref
+    out["note"] = ("tc: k_gemm_tc (tcgen05.mma, TMEM accumulator, cp.async.bulk.tensor operands, operands made "
+                   "K-major first where a transpose is needed, included in the time); mma_sync: k_gemm_bf16; "
+                   "fractions of the measured cuBLAS BF16 burst rate")
+    return out
+
+
 def learned_section(steps=200, train_steps=50, epochs=20):
     """Learned initial iterate on the multigroup Marshak wave: steps 1..train_steps
     plain (their (state -> next moments) pairs recorded), then a per-cell MLP
@@ -829,6 +883,7 @@ def run_gpu(args):
         line["chive_2d"] = chive2d_section(cpu=not args.no_cpu)
         line["trt_marshak"] = trt_section(args.trt_steps)
         line["learned_iterate"] = learned_section(args.trt_steps, min(50, args.trt_steps // 4))
+        line["mlp_gemm"] = gemm_section()
         if args.batch_problems > 0:
             line["batched_uneven"] = batch_section(args.batch_problems)
     if not args.no_cpu and tuple(cells) == CELLS:
@@ -862,9 +917,12 @@ def main():
                     help="sweep schedule: chosen by the autotuner, or fixed (for profiler runs, whose "
                          "serialised launches would skew the tuner)")
     ap.add_argument("--batch-problems", type=int, default=256, help="problems of the batched section (0 skips it)")
+    ap.add_argument("--gemm", action="store_true", help="only the MLP GEMM comparison (one JSON line)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.gemm:
+        print(json.dumps({"mlp_gemm": gemm_section()}), flush=True)
     else:
         run_gpu(args)
 

@@ -492,6 +492,25 @@ int allium_mlp_gemm(int M, int N, int K, const void* A, long long sam, long long
                     long long sbn, float* C, long long ldc, void* C_bf16, const float* bias, float alpha, float beta,
                     int relu, void* stream);
 
+/* C[M][N] = alpha A[M][K] B[N][K]^T (+ beta C) (+ bias[N]) (ReLU) on the
+ * fifth-generation tensor cores (tcgen05.mma, FP32 accumulator in tensor
+ * memory, operands streamed by cp.async.bulk.tensor).  A and B are BF16 with K
+ * contiguous; their row strides lda, ldb are multiples of 8 elements and their
+ * base addresses 16-byte aligned (ALLIUM_ERR_ARG otherwise).  C row stride
+ * ldc, C_bf16 (row stride ldcb) receives a BF16 copy when not NULL.  ksplit > 1
+ * splits K over that many tiles' worth of blocks and adds the partial sums into
+ * C, which the call zeroes first (C only: no bias, ReLU, beta or BF16 copy). */
+int allium_mlp_gemm_tc(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, float* C,
+                       long long ldc, void* C_bf16, long long ldcb, const float* bias, float alpha, float beta, int relu,
+                       int ksplit, void* stream);
+
+/* out[c][r] = in[r][c] for a rows x cols BF16 matrix (row strides ldi, ldo). */
+int allium_mlp_transpose_bf16(int rows, int cols, const void* in, long long ldi, void* out, long long ldo, void* stream);
+
+/* Synchronizes the stream; ALLIUM_ERR_TIMEOUT (and the word cleared) if a
+ * bounded wait inside allium_mlp_gemm_tc gave up since the last call. */
+int allium_mlp_status(void* stream);
+
 /* dz = dy where y > 0, else 0 (ReLU gradient); dz and/or its BF16 copy. */
 int allium_mlp_relu_backward(long long count, const float* dy, const float* y, float* dz, void* dz_bf16, void* stream);
 

@@ -15,11 +15,15 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("tc", [True, False])
 @pytest.mark.parametrize("M,N,K,ta,tb", [(1, 1, 1, False, False), (70, 33, 45, False, False),
                                          (300, 256, 128, False, False), (45, 70, 33, True, False),
-                                         (64, 96, 200, False, True), (129, 65, 300, True, True)])
-def test_gemm(M, N, K, ta, tb):
-    from allium_gb300.mlp import gemm
+                                         (64, 96, 200, False, True), (129, 65, 300, True, True),
+                                         (1000, 384, 712, False, True)])
+def test_gemm(M, N, K, ta, tb, tc):
+    # tc: the tcgen05 kernel (TMEM accumulator, operands by cp.async.bulk.tensor);
+    # else the mma.sync kernel
+    from allium_gb300.mlp import gemm, tc_status
     rng = np.random.default_rng(M + N + K)
     A = rng.normal(size=(K, M) if ta else (M, K)).astype(np.float32)
     B = rng.normal(size=(N, K) if tb else (K, N)).astype(np.float32)
@@ -28,7 +32,9 @@ def test_gemm(M, N, K, ta, tb):
     dA = torch.from_numpy(A).cuda().to(torch.bfloat16)
     dB = torch.from_numpy(B).cuda().to(torch.bfloat16)
     out = torch.from_numpy(C0.copy()).cuda()
-    gemm(dA, dB, out=out, bias=torch.from_numpy(bias).cuda(), relu=True, alpha=0.5, beta=2.0, transA=ta, transB=tb)
+    gemm(dA, dB, out=out, bias=torch.from_numpy(bias).cuda(), relu=True, alpha=0.5, beta=2.0, transA=ta, transB=tb,
+         tc=tc)
+    tc_status()
     a = bf16(A).T if ta else bf16(A)
     b = bf16(B).T if tb else bf16(B)
     ref = np.maximum(0.5 * (a @ b) + 2.0 * C0 + bias, 0.0)
@@ -90,16 +96,18 @@ def test_learned_iterate_keeps_answers():
         assert err < 1e-6
 
 
+@pytest.mark.parametrize("tc", [True, False])
 @pytest.mark.parametrize("M,N,K,ta", [(37, 64, 5000, True), (133, 256, 16384, True), (64, 64, 300, False)])
-def test_gemm_split_k(M, N, K, ta):
+def test_gemm_split_k(M, N, K, ta, tc):
     # few output tiles over a long K: the kernel splits K over blocks and adds
     # the partial sums atomically (the weight gradients X^T dY over a batch)
-    from allium_gb300.mlp import gemm
+    from allium_gb300.mlp import gemm, tc_status
     rng = np.random.default_rng(K)
     A = rng.normal(size=(K, M) if ta else (M, K)).astype(np.float32)
     B = rng.normal(size=(K, N)).astype(np.float32)
     out = gemm(torch.from_numpy(A).cuda().to(torch.bfloat16), torch.from_numpy(B).cuda().to(torch.bfloat16),
-               transA=ta)
+               transA=ta, tc=tc)
+    tc_status()
     a = bf16(A).T if ta else bf16(A)
     ref = a @ bf16(B)
     assert np.max(np.abs(out.cpu().numpy() - ref)) <= 1e-5 * np.max(np.abs(ref))
