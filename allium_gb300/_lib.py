@@ -75,6 +75,7 @@ EXPORTS = {
                                               C.c_void_p, C.c_void_p]),
     "allium_sweep_fused_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "allium_sweep_set_fused_pdl": (C.c_int, [C.c_void_p, C.c_int]),
+    "allium_sweep_set_level_pdl": (C.c_int, [C.c_void_p, C.c_int]),
     "allium_sweep_transport_residual_df": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                      C.c_void_p, C.c_void_p, C.c_void_p]),
     "allium_sweep_moments_df": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -664,6 +664,13 @@ int allium_sweep_fused_levels(allium_sweep* s, int* num_levels, int* unit_levels
     return ALLIUM_OK;
 }
 
+int allium_sweep_set_level_pdl(allium_sweep* s, int on) {
+    if (!s) return ALLIUM_ERR_ARG;
+    allium::drop_graphs(s->h);
+    s->h.pdl_levels = on ? 1 : 0;
+    return ALLIUM_OK;
+}
+
 int allium_sweep_set_fused_pdl(allium_sweep* s, int on) {
     if (!s) return ALLIUM_ERR_ARG;
     allium::set_fused_pdl(s->h, on);

@@ -23,14 +23,15 @@
 //
 // k_fused_level work unit: one thread per (cell, angle, group) node of a level.
 // Nodes come from a record {cell, angle | face pattern << 16}, sorted within
-// each level by (cell, face pattern, angle) and packed so that a warp holds at
-// most kSlots cells (padding records {-1, 0} close a warp early).  Each warp
-// copies the FP32 tables of its cells (G_d, M, [Mt], F_k and the outward face
-// normals, 1.5 KB for a trilinear hex) into shared memory with cp.async.bulk
-// and an mbarrier per copy, one slot per cell, while its lanes load their
+// each level by (cell, unit, angle) and packed so that a warp holds at most
+// kSlots units (padding records {-1, 0} close a warp early).  Each warp copies
+// the FP32 tables of its units (B_d = G_d + the unit's outflow-face terms
+// n_{k,d} F_k, M, [Mt], F_k and the outward face normals, 1.5 KB for a
+// trilinear hex) into shared memory with cp.async.bulk and an mbarrier per
+// copy, one slot per unit, while its lanes load their
 // sources and, after griddepcontrol.wait, their upwind traces (one 32-byte
 // neighbour block per inflow face when the face's DOF map is the standard
-// one), folded into the right-hand side as they arrive.  Each row of the local
+// one), folded into the right-hand side with the staged face blocks.  Each row of the local
 // system is then assembled from shared memory with packed FP32 (f32x2) FMAs,
 // eliminated against the rows above and scaled by its pivot's reciprocal, so
 // that only the strict upper triangle of a unit-diagonal U stays in registers.
@@ -439,6 +440,14 @@ struct FusedState {
     float* w = nullptr;              // [Nw] FP32 weights
     float* tab = nullptr;            // [ne][Tab::size]
     int tab_td = -1;                 // time mass included in tab (-1: not built)
+    // per-unit tables for the sweep: the cell's table with G_d replaced by
+    // B_d = G_d + sum over the unit's outflow faces k of n_{k,d} F_k
+    float* utab = nullptr;           // [nunits][Tab::size]
+    int utab_td = -1;
+    int nunits = 0;
+    int* unit_cell = nullptr;        // [nunits] cell of each unit
+    int* unit_pat = nullptr;         // [nunits] face pattern of each unit
+    int* rec_unit = nullptr;         // [records] unit of each record (-1 on padding)
     float* dtab = nullptr;           // [ne][DTab::size]
     int dtab_td = -1;
     float2* ddots = nullptr;         // [nfaces][Nw] double-float Omega . n
@@ -491,16 +500,56 @@ __global__ void k_fused_nodes(long long n, int Nw, int dim, const double* __rest
 // sort key of a record: (level, cell, face pattern); the sort is stable, so
 // each (cell, pattern) keeps its angles in order.  level_of is indexed by unit
 // (unit_of_node given) or by node e Nw + a.
+// sort key of a node record: (level, unit); units are numbered cell by cell, so
+// a level's records come out grouped by cell, then unit, then (stable) angle
 __global__ void k_fused_keys(long long n, int Nw, const int2* __restrict__ recs, const int* __restrict__ level_of,
-                             const int* __restrict__ unit_of_node, unsigned long long* __restrict__ keys) {
+                             bool unit_levels, const int* __restrict__ unit_of_node,
+                             unsigned long long* __restrict__ keys) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int2 r = recs[t];
     const int a = r.y & 0xffff;
-    const unsigned pat = (unsigned)r.y >> 16;
     const long long v = (long long)r.x * Nw + a;
-    const int lev = unit_of_node ? level_of[unit_of_node[v]] : level_of[v];
-    keys[t] = ((unsigned long long)lev << 36) | ((unsigned long long)r.x << 12) | pat;
+    const int u = unit_of_node[v];
+    const int lev = unit_levels ? level_of[u] : level_of[v];
+    keys[t] = ((unsigned long long)lev << 36) | (unsigned long long)(unsigned)u;
+}
+
+// cell and face pattern of every unit (all nodes of a unit share both)
+__global__ void k_unit_info(long long n, int Nw, const int2* __restrict__ recs, const int* __restrict__ unit_of_node,
+                            int* __restrict__ unit_cell, int* __restrict__ unit_pat) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int u = unit_of_node[v];
+    unit_cell[u] = recs[v].x;
+    unit_pat[u] = (int)((unsigned)recs[v].y >> 16);
+}
+
+// per-unit table: the cell's table with each G_d row replaced by
+// B_d = G_d + sum_{outflow faces k} n_{k,d} F_k (F_k at the face's DOFs), so that
+// A = sum_d Omega_d B_d + sigma M [+ tau Mt] for every angle of the unit
+template <int D, int P, bool TD>
+__global__ void k_unit_tab(int nu, const int* __restrict__ unit_cell, const int* __restrict__ unit_pat,
+                           const float* __restrict__ tab, float* __restrict__ utab) {
+    using S = Shape<D, P>;
+    using T = Tab<D, P, TD>;
+    constexpr int N = S::N, NF = S::NF, NFACE = S::NFACE;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nu * T::size) return;
+    const int u = (int)(t / T::size), o = (int)(t % T::size);
+    const float* ct = tab + (size_t)unit_cell[u] * T::size;
+    float v = ct[o];
+    if (o < T::oM) {
+        const int d = o / (N * N), i = (o / N) % N, j = o % N;
+        const int pat = unit_pat[u];
+        for (int k = 0; k < NFACE; ++k) {
+            if (((pat >> (2 * k)) & 3) != 1) continue;
+            const int ii = face_pos(D, P, k, i), jj = face_pos(D, P, k, j);
+            if (ii < 0 || jj < 0) continue;
+            v = fmaf(ct[T::oNrm + 4 * k + d], ct[T::oF + (k * NF + ii) * NF + jj], v);
+        }
+    }
+    utab[t] = v;
 }
 
 // first record of each level in the sorted keys (level in bits 36 and up)
@@ -610,17 +659,15 @@ __global__ void k_unit_kahn(int Nw, int dim, const int* __restrict__ key, const 
 }
 
 // Packing of a level's records into warps of 32 lanes that hold at most
-// kSlots cells each: a cell's run of records that would be a warp's
-// kSlots+1-th cell starts the next warp instead, and each level is padded to
-// whole warps with records {-1, 0}.  Runs (records of one cell within one
-// level, consecutive after the sort) are found in parallel; the greedy
-// placement walks a level's runs in one thread; the records are then scattered
-// in parallel.
-__global__ void k_run_flags(long long n, const unsigned long long* __restrict__ keys, const int2* __restrict__ recs,
-                            int* __restrict__ flag) {
+// kSlots units (tables) each: a unit's run of records that would be a warp's
+// kSlots+1-th starts the next warp instead, and each level is padded to whole
+// warps with records {-1, 0}.  Runs (records of one unit within one level,
+// consecutive after the sort) are found in parallel; the greedy placement walks
+// a level's runs in one thread; the records are then scattered in parallel.
+__global__ void k_run_flags(long long n, const unsigned long long* __restrict__ keys, int* __restrict__ flag) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    flag[i] = (i == 0 || (keys[i] >> 36) != (keys[i - 1] >> 36) || recs[i].x != recs[i - 1].x) ? 1 : 0;
+    flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;   // a run: one unit within one level
 }
 
 // run_start[r] = first record of run r (flag[i] == 1, ridx[i] its exclusive scan)
@@ -643,7 +690,7 @@ __global__ void k_pack_runs(int nlev, long long n, int nruns, const long long* _
     const int r0 = ridx[starts[l]];
     const int r1 = starts[l + 1] < n ? ridx[starts[l + 1]] : nruns;
     long long pos = 0;
-    int cells = 0;   // cells touching the warp that holds lane pos
+    int cells = 0;   // runs (units) touching the warp that holds lane pos
     for (int r = r0; r < r1; ++r) {
         const long long len = (long long)(r + 1 < nruns ? run_start[r + 1] : n) - run_start[r];
         if ((pos & 31) == 0) cells = 0;
@@ -658,20 +705,25 @@ __global__ void k_pack_runs(int nlev, long long n, int nruns, const long long* _
     sizes[l] = (pos + 31) & ~31LL;
 }
 
-__global__ void k_pack_fill(long long n, int2* __restrict__ out) {
+__global__ void k_pack_fill(long long n, int2* __restrict__ out, int* __restrict__ out_unit) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_int2(-1, 0);
+    if (i >= n) return;
+    out[i] = make_int2(-1, 0);
+    out_unit[i] = -1;
 }
 
 __global__ void k_pack_scatter(long long n, const unsigned long long* __restrict__ keys, const int2* __restrict__ recs,
                                const int* __restrict__ ridx, const int* __restrict__ flag,
                                const int* __restrict__ run_start, const int* __restrict__ run_pos,
-                               const long long* __restrict__ out_starts, int2* __restrict__ out) {
+                               const long long* __restrict__ out_starts, int2* __restrict__ out,
+                               int* __restrict__ out_unit) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int r = ridx[i] + flag[i] - 1;   // run of record i (inclusive scan - 1)
     const int l = (int)(keys[i] >> 36);
-    out[out_starts[l] + run_pos[r] + (i - run_start[r])] = recs[i];
+    const long long o = out_starts[l] + run_pos[r] + (i - run_start[r]);
+    out[o] = recs[i];
+    out_unit[o] = (int)(keys[i] & 0xFFFFFFFFull);
 }
 
 __global__ void k_fused_cells(int ne, int dim, int p, int nf, const Slot* __restrict__ slots,
@@ -801,7 +853,9 @@ __global__ void k_iso_source(int ne, int G, int N, double wsum, const double* __
 struct FusedArgs {
     int ne, Nw, G;
     const int2* nodes;
-    const float* tab;
+    const int* rec_unit;     // unit of each record
+    int nunits;
+    const float* tab;        // per-unit tables
     const int* nbr;
     const unsigned* map;
     const float4* omega;
@@ -828,7 +882,7 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
     const long long total = (long long)count * f.G;
     const long long t = (long long)blockIdx.x * kSweepBlock + threadIdx.x;
     bool valid = false;
-    int g = 0, e = 0, a = 0, pat = 0;
+    int g = 0, e = 0, a = 0, pat = 0, u = 0;
     if (t < total) {
         g = (int)(t / count);
         const int ni = (int)(t - (long long)g * count);
@@ -837,11 +891,12 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
         e = valid ? r.x : 0;
         a = r.y & 0xffff;
         pat = (int)((unsigned)r.y >> 16);
+        u = valid ? f.rec_unit[base + ni] : 0;
     }
     float* wtab = s_tab + warp * kSlots * T::size;
     unsigned long long* wbar = s_bar + warp * kSlots;
     bool start = false;
-    const int run = stage_runs<kSlots>(wtab, wbar, f.tab, T::size, valid, g * f.ne + e, e, start);
+    const int run = stage_runs<kSlots>(wtab, wbar, f.tab, T::size, valid, g * f.nunits + u, u, start);
 
     // loads that do not depend on the previous levels
     float b[N];
@@ -864,19 +919,19 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
 #pragma unroll
         for (int k = 0; k < NFACE; ++k)
             if (((pat >> (2 * k)) & 3) == 2) nb[k] = f.nbr[(size_t)e * NFACE + k];
-        // the cell's face blocks and normals into L1 for the inflow fold below
-        // (griddepcontrol.wait is a compiler barrier, so those loads come after it)
-        const char* ft = reinterpret_cast<const char*>(f.tab + (size_t)e * T::size + T::oF);
-#pragma unroll
-        for (int off = 0; off < 4 * (T::size - T::oF); off += 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(ft + off));
     }
-    // the upwind traces were written by earlier levels: fold each inflow face's
-    // term |Omega.n| F_k u_k into b as its trace arrives (the face block and
-    // normal through L1 from the cell's table, which the warp shares), so that
-    // no trace stays live across the table wait
+    // the upwind traces were written by earlier levels: after the wait, fold each
+    // inflow face's term |Omega.n| F_k u_k into b as its trace arrives, the face
+    // block and normal read from the cell's staged table.  The schedule packs at
+    // most kSlots cells into a warp, so every table of the warp was staged by
+    // stage_runs.
     griddep_wait();
-    if (valid) {
-        const float* gt = f.tab + (size_t)e * T::size;
+    const bool staged = valid && run < kSlots;
+    if (valid && !staged) atomicOr(f.status, kErrSchedule);
+    unsigned tb = 0;
+    if (staged) {
+        wait_copy(&wbar[run], 0u, f.status);
+        tb = smem_u32(wtab + run * T::size);
         sfor<0, NFACE>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
             if (((pat >> (2 * k)) & 3) == 2) {
@@ -895,7 +950,7 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
 #pragma unroll
                     for (int jj = 0; jj < NF; ++jj) u[jj] = __ldcg(up + ((m4 >> (8 * jj)) & 0xffu));
                 }
-                const float4 nr = __ldg(reinterpret_cast<const float4*>(gt + T::oNrm + 4 * k));
+                const float4 nr = lds4(tb + 4u * (T::oNrm + 4 * k));
                 float d = om.x * nr.x;
                 if (D > 1) d = fmaf(om.y, nr.y, d);
                 if (D > 2) d = fmaf(om.z, nr.z, d);
@@ -903,7 +958,7 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
                 sfor<0, NF>([&](auto ic) {
                     constexpr int ii = decltype(ic)::value;
                     float fr[NF];
-                    ld_vec<NF>(gt + T::oF + (k * NF + ii) * NF, fr);
+                    lds_vec<NF>(tb + 4u * (T::oF + (k * NF + ii) * NF), fr);
                     float acc = 0.f;
 #pragma unroll
                     for (int jj = 0; jj < NF; ++jj) acc = fmaf(fr[jj], u[jj], acc);
@@ -914,28 +969,10 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
         });
     }
 
-    // the schedule packs at most kSlots cells into a warp, so every table of the
-    // warp was staged by stage_runs
-    const bool staged = valid && run < kSlots;
-    if (valid && !staged) atomicOr(f.status, kErrSchedule);
     if (staged) {
-        wait_copy(&wbar[run], 0u, f.status);
-        const unsigned tb = smem_u32(wtab + run * T::size);
         const float omv[3] = {om.x, om.y, om.z};
-        // |Omega.n| on the outflow faces
-        float dk[NFACE];
-#pragma unroll
-        for (int k = 0; k < NFACE; ++k) {
-            dk[k] = 0.f;
-            if (((pat >> (2 * k)) & 3) == 1) {
-                const float4 nr = lds4(tb + 4u * (T::oNrm + 4 * k));
-                float d = omv[0] * nr.x;
-                if (D > 1) d = fmaf(omv[1], nr.y, d);
-                if (D > 2) d = fmaf(omv[2], nr.z, d);
-                dk[k] = fabsf(d);
-            }
-        }
-        // rows of A = sum_d Omega_d G_d + sigma M [+ tau Mt] + sum_{outflow} |Omega.n| F_k,
+        // rows of A = sum_d Omega_d B_d + sigma M [+ tau Mt], B_d = G_d + sum_{outflow k}
+        // n_{k,d} F_k from the unit's table (on an outflow face Omega.n = |Omega.n|),
         // assembled one at a time, eliminated against the rows above (no pivoting)
         // and scaled by their pivot's reciprocal: only the strict upper triangle of
         // the unit-diagonal U (and the scaled right-hand side) stays live
@@ -961,20 +998,6 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
 #pragma unroll
                 for (int p = 0; p < NP; ++p) ar[p] = fma2(f2(f.tau), tr[p], ar[p]);
             }
-            sfor<0, NFACE>([&](auto kc) {
-                constexpr int k = decltype(kc)::value;
-                constexpr int ii = face_pos(D, P, k, i);
-                if constexpr (ii >= 0) {
-                    if (((pat >> (2 * k)) & 3) == 1) {
-                        float fr[NF];
-                        lds_vec<NF>(tb + 4u * (T::oF + (k * NF + ii) * NF), fr);
-                        sfor<0, NF>([&](auto jc) {
-                            constexpr int jj = decltype(jc)::value;
-                            fma_to(ar, face_dof(D, P, k, jj), dk[k], fr[jj]);
-                        });
-                    }
-                }
-            });
             float y = b[i];
             sfor<0, i>([&](auto mc) {
                 constexpr int m = decltype(mc)::value;
@@ -1436,6 +1459,29 @@ cudaError_t build_dtab(Handle& h, FusedState& fs) {
     return cudaSuccess;
 }
 
+template <int D, int P, bool TD>
+cudaError_t build_utab(Handle& h, FusedState& fs) {
+    using T = Tab<D, P, TD>;
+    if (fs.utab) { cudaFree(fs.utab); fs.utab = nullptr; }
+    FCK(cudaMalloc(&fs.utab, (size_t)fs.nunits * T::size * sizeof(float)));
+    const long long n = (long long)fs.nunits * T::size;
+    k_unit_tab<D, P, TD><<<blocks(n, 256), 256, 0, h.stream>>>(fs.nunits, fs.unit_cell, fs.unit_pat, fs.tab, fs.utab);
+    FCK(cudaGetLastError());
+    fs.utab_td = TD ? 1 : 0;
+    return cudaSuccess;
+}
+
+cudaError_t dispatch_utab(Handle& h, FusedState& fs) {
+    const bool td = h.time_dependent;
+#define UTAB_CASE(D_, P_) \
+    case D_ * 10 + P_: return td ? build_utab<D_, P_, true>(h, fs) : build_utab<D_, P_, false>(h, fs);
+    switch (h.dim * 10 + h.p) {
+        UTAB_CASE(1, 0) UTAB_CASE(1, 1) UTAB_CASE(2, 0) UTAB_CASE(2, 1) UTAB_CASE(3, 0) UTAB_CASE(3, 1)
+        default: return cudaErrorNotSupported;
+    }
+#undef UTAB_CASE
+}
+
 template <bool DF>
 cudaError_t dispatch_tab(Handle& h, FusedState& fs) {
     const bool td = h.time_dependent;
@@ -1450,12 +1496,13 @@ cudaError_t dispatch_tab(Handle& h, FusedState& fs) {
 #undef TAB_CASE
 }
 
-// Unit levels: level of every unit and unit of every node, or *nlev = -1 when
-// a cell has more than kMaxUnits units or the unit graph has a cycle (the
-// caller then keeps the node levels).
-cudaError_t unit_levels(Handle& h, int** unit_of_node, int** level_of_unit, int* nlev) {
+// Unit levels: unit of every node (*nunits units, 0 when a cell has more than
+// kMaxUnits units) and level of every unit, or *nlev = -1 when there are no
+// units or the unit graph has a cycle (the caller then keeps the node levels).
+cudaError_t unit_levels(Handle& h, int** unit_of_node, int** level_of_unit, int* nlev, int* nunits) {
     const long long N = (long long)h.ne * h.Nw;
     *nlev = -1;
+    *nunits = 0;
     *unit_of_node = nullptr;
     *level_of_unit = nullptr;
     int *key = nullptr, *nin = nullptr, *unit = nullptr, *cnt = nullptr, *base = nullptr, *flag = nullptr;
@@ -1467,12 +1514,17 @@ cudaError_t unit_levels(Handle& h, int** unit_of_node, int** level_of_unit, int*
         void* bufs[] = {key, nin, cnt, base, flag, pending, usize, ustart, ufill, unodes, fa, fb, fc, tmp};
         for (void* b : bufs)
             if (b) cudaFree(b);
-        if (*nlev < 0 || e != cudaSuccess) {
+        if (e != cudaSuccess || *nunits == 0) {
             *nlev = -1;
+            *nunits = 0;
             cudaFree(unit);
             cudaFree(ulevel);
+            return e;
+        }
+        *unit_of_node = unit;
+        if (*nlev < 0) {
+            cudaFree(ulevel);
         } else {
-            *unit_of_node = unit;
             *level_of_unit = ulevel;
         }
         return e;
@@ -1502,6 +1554,7 @@ cudaError_t unit_levels(Handle& h, int** unit_of_node, int** level_of_unit, int*
     UCK(cudaStreamSynchronize(h.stream));
     if (host[0]) return finish(cudaSuccess);   // too many units in a cell
     const int nu = host[1] + host[2];
+    *nunits = nu;
     UCK(cudaMalloc(&pending, (size_t)nu * sizeof(int)));
     UCK(cudaMalloc(&usize, (size_t)nu * sizeof(int)));
     UCK(cudaMalloc(&ustart, (size_t)nu * sizeof(int)));
@@ -1561,8 +1614,13 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     if (h.ne >= (1 << 24) || h.num_levels >= (1 << 27) || N > 0x7fffffffLL) return cudaErrorInvalidValue;
     int* unit = nullptr;
     int* ulevel = nullptr;
-    int nlev = -1;
-    FCK(unit_levels(h, &unit, &ulevel, &nlev));
+    int nlev = -1, nunits = 0;
+    FCK(unit_levels(h, &unit, &ulevel, &nlev, &nunits));
+    if (nunits == 0 || (long long)h.G * nunits >= (1LL << 31)) {   // more than kMaxUnits units in a cell
+        cudaFree(unit);
+        cudaFree(ulevel);
+        return cudaErrorNotSupported;
+    }
     const int* level_of = ulevel;
     fs.unit_levels = nlev >= 0 && nlev < (1 << 27);
     if (!fs.unit_levels) {
@@ -1604,8 +1662,13 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     step(cudaMalloc(&starts, (nlev + 1) * sizeof(long long)));
     if (err == cudaSuccess) {
         k_fused_nodes<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, h.dim, h.d_dots, h.d_slots, recs);
-        k_fused_keys<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, recs, level_of, fs.unit_levels ? unit : nullptr,
-                                                           keys);
+        k_fused_keys<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, recs, level_of, fs.unit_levels, unit, keys);
+        step(cudaGetLastError());
+    }
+    step(cudaMalloc(&fs.unit_cell, (size_t)nunits * sizeof(int)));
+    step(cudaMalloc(&fs.unit_pat, (size_t)nunits * sizeof(int)));
+    if (err == cudaSuccess) {
+        k_unit_info<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, recs, unit, fs.unit_cell, fs.unit_pat);
         step(cudaGetLastError());
     }
     if (err == cudaSuccess)
@@ -1621,7 +1684,7 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     }
     // warps of at most kSlots cells: runs, their padded positions, level sizes, records
     if (err == cudaSuccess) {
-        k_run_flags<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, sorted, flag);
+        k_run_flags<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, flag);
         step(cudaGetLastError());
     }
     if (err == cudaSuccess) step(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, flag, ridx, (int)N, h.stream));
@@ -1649,12 +1712,13 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
         if (ps[nlev] > 0x7fffffffLL) err = cudaErrorInvalidValue;
     }
     if (err == cudaSuccess) step(cudaMalloc(&fs.nodes, (size_t)ps[nlev] * sizeof(int2)));
+    if (err == cudaSuccess) step(cudaMalloc(&fs.rec_unit, (size_t)ps[nlev] * sizeof(int)));
     if (err == cudaSuccess)
         step(cudaMemcpyAsync(pstart, ps.data(), (nlev + 1) * sizeof(long long), cudaMemcpyHostToDevice, h.stream));
     if (err == cudaSuccess) {
-        k_pack_fill<<<blocks(ps[nlev], 256), 256, 0, h.stream>>>(ps[nlev], fs.nodes);
+        k_pack_fill<<<blocks(ps[nlev], 256), 256, 0, h.stream>>>(ps[nlev], fs.nodes, fs.rec_unit);
         k_pack_scatter<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, sorted, ridx, flag, run_start, run_pos,
-                                                             pstart, fs.nodes);
+                                                             pstart, fs.nodes, fs.rec_unit);
         step(cudaGetLastError());
     }
     if (err == cudaSuccess) step(cudaStreamSynchronize(h.stream));
@@ -1670,13 +1734,15 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
         step(cudaGetLastError());
     }
     if (err != cudaSuccess) {
-        void* bufs[] = {fs.nodes, fs.nbr, fs.map, fs.omega, fs.w, fs.domega, fs.dw};
+        void* bufs[] = {fs.nodes, fs.nbr, fs.map, fs.omega, fs.w, fs.domega, fs.dw, fs.rec_unit, fs.unit_cell,
+                        fs.unit_pat};
         for (void* b : bufs)
             if (b) cudaFree(b);
         fs.nodes = nullptr; fs.nbr = nullptr; fs.map = nullptr; fs.omega = nullptr; fs.w = nullptr;
-        fs.domega = nullptr; fs.dw = nullptr;
+        fs.domega = nullptr; fs.dw = nullptr; fs.rec_unit = nullptr; fs.unit_cell = nullptr; fs.unit_pat = nullptr;
         return err;
     }
+    fs.nunits = nunits;
     fs.num_levels = nlev;
     fs.level_offsets.assign(nlev + 1, 0);
     for (int l = 0; l <= nlev; ++l) fs.level_offsets[l] = (int)ps[l];
@@ -1799,7 +1865,8 @@ void free_fused(Handle& h) {
     if (!h.fused) return;
     drop_fused_graphs(h);
     FusedState& fs = *h.fused;
-    void* bufs[] = {fs.nodes, fs.nbr, fs.map, fs.omega, fs.w, fs.tab, fs.dtab, fs.ddots, fs.domega, fs.dw, fs.dsigma};
+    void* bufs[] = {fs.nodes, fs.nbr, fs.map, fs.omega, fs.w, fs.tab, fs.dtab, fs.ddots, fs.domega, fs.dw, fs.dsigma,
+                    fs.utab, fs.unit_cell, fs.unit_pat, fs.rec_unit};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete h.fused;
@@ -1816,9 +1883,14 @@ cudaError_t launch_fused_sweep(Handle& h, const float* iso, const float* src, fl
         drop_fused_graphs(h);
         FCK(dispatch_tab<false>(h, fs));
     }
+    if (fs.utab_td != td) {
+        drop_fused_graphs(h);
+        FCK(dispatch_utab(h, fs));
+    }
     FusedArgs a;
     a.ne = h.ne; a.Nw = h.Nw; a.G = h.G;
-    a.nodes = fs.nodes; a.tab = fs.tab; a.nbr = fs.nbr; a.map = fs.map;
+    a.nodes = fs.nodes; a.tab = fs.utab; a.nbr = fs.nbr; a.map = fs.map;
+    a.rec_unit = fs.rec_unit; a.nunits = fs.nunits;
     a.omega = fs.omega; a.sigma = h.f_sigma; a.tau = (float)h.tau;
     a.iso = iso; a.src = src; a.psi = psi;
     a.acc_hi = acc_hi; a.acc_lo = acc_hi ? acc_lo : nullptr;

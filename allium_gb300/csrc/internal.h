@@ -91,6 +91,7 @@ struct Handle {
 
     // threads per block of the thread-per-node level kernels (FP64, FP32)
     int block64 = 128, block32 = 128;
+    int pdl_levels = 1;   // programmatic dependent launch between stored-inverse level launches
     double *d_G = nullptr, *d_M = nullptr, *d_Mt = nullptr, *d_F = nullptr, *d_sigma = nullptr;
     float *f_G = nullptr, *f_M = nullptr, *f_Mt = nullptr, *f_F = nullptr, *f_sigma = nullptr;
     int* d_level = nullptr;          // [ne*Nw]

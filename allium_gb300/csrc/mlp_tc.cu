@@ -5,14 +5,16 @@
 // One CTA of 128 threads owns a 128 x BN tile of C (BN = 256 when N > 128, else
 // 128); its accumulator lives in tensor memory (128 lanes x BN FP32 columns).
 // Warp 0's elected lane streams 128 x 64 tiles of A and BN x 64 tiles of B into
-// a shared-memory ring (four stages of 48 KB, or six of 32 KB) with
+// a shared-memory ring (two stages of 48 KB, or three of 32 KB) with
 // cp.async.bulk.tensor (128-byte swizzle, out-of-range rows and columns
 // zero-filled by the tensor map); warp 1's elected lane issues
 // tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = BN, K = 16, four per stage)
 // and frees each stage with tcgen05.commit on the stage's mbarrier.  After the
 // last commit every warp reads its 32 accumulator lanes with tcgen05.ld and
-// applies the epilogue through shared memory (coalesced row stores).  With ksplit > 1, blockIdx.z takes one of ksplit K
-// ranges and the partial sums are added atomically (C zeroed beforehand).
+// applies the epilogue through shared memory (coalesced row stores).  Two CTAs
+// share an SM, so one's epilogue overlaps the other's MMAs.  With ksplit > 1,
+// blockIdx.z takes one of ksplit K ranges and the partial sums are added
+// atomically (C zeroed beforehand).
 //
 // Every mbarrier wait is bounded; a wait that gives up sets the module's status
 // word (allium_mlp_status), and the epilogue waits once more (bounded) for the
@@ -33,10 +35,12 @@ constexpr int TILE_A_BYTES = TM * TK * 2;            // 16 KB
 constexpr int kWaitLimit = 1 << 22;
 
 // tile N (128 or 256: the accumulator's FP32 columns in tensor memory) and the
-// ring depth; both shapes use 192 KB of shared memory for the ring
+// ring depth; both shapes use 96 KB of shared memory, so that two CTAs share an
+// SM (and its 512 tensor-memory columns) and one's epilogue overlaps the other's
+// MMAs
 template <int BN>
 struct TcShape {
-    static constexpr int STAGES = BN == 256 ? 4 : 6;
+    static constexpr int STAGES = BN == 256 ? 2 : 3;
     static constexpr int TILE_B_BYTES = BN * TK * 2;
     static constexpr int STAGE_BYTES = TILE_A_BYTES + TILE_B_BYTES;
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
@@ -87,7 +91,7 @@ __device__ __forceinline__ uint64_t sw128_desc(unsigned saddr) {
 }
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tA,
+__global__ void __launch_bounds__(128, 2) k_gemm_tc(const __grid_constant__ CUtensorMap tA,
                                                     const __grid_constant__ CUtensorMap tB, TcArgs g) {
     using Sh = TcShape<BN>;
     constexpr int STAGES = Sh::STAGES, STAGE_BYTES = Sh::STAGE_BYTES;

@@ -71,15 +71,29 @@ template <int D, int P, typename R>
 cudaError_t sweep_levels_cached(Handle& h, const SweepArgs<R>& args, const R* inv, cudaStream_t stream) {
     const int kBlock = std::is_same<R, double>::value ? h.block64 : h.block32;
     const long long stride = (long long)h.G * h.ne * h.Nw;
+    // every level after the first may start its blocks while the previous one
+    // drains (programmatic dependent launch); they wait before reading upwind data
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    bool first = true;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = h.h_level_offsets[l];
         const int count = h.h_level_offsets[l + 1] - off;
         if (count == 0) continue;
         const long long threads = (long long)count * h.G;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
-        const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_cached_level<D, P, R><<<grid, kBlock, 0, stream>>>(args, h.d_level_nodes + off, count, inv, stride,
-                                                                   (long long)off * h.G, nullptr);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)((threads + kBlock - 1) / kBlock));
+        cfg.blockDim = dim3(kBlock);
+        cfg.stream = stream;
+        cfg.attrs = attr;
+        cfg.numAttrs = (h.pdl_levels && !first) ? 1 : 0;
+        cudaError_t e = cudaLaunchKernelEx(&cfg, k_sweep_cached_level<D, P, R, false>, args,
+                                           (const int*)(h.d_level_nodes + off), count, inv, stride,
+                                           (long long)off * h.G, (const int*)nullptr);
+        if (e != cudaSuccess) return e;
+        first = false;
     }
     return cudaGetLastError();
 }
@@ -92,15 +106,27 @@ cudaError_t sweep_chunk(Handle& h, const SweepArgs<double>& args, int c, cudaStr
     const int kBlock = h.block64;
     const long long stride = (long long)h.G * h.ne * h.Nw;
     const int* offs = h.h_chunk_offsets.data() + (size_t)c * (h.num_levels + 1);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    bool first = true;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = offs[l];
         const int count = offs[l + 1] - off;
         if (count == 0) continue;
         const long long threads = (long long)count * h.G;
         if (threads > 0x7fffffffLL) return cudaErrorInvalidValue;
-        const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-        k_sweep_cached_level<D, P, double, true><<<grid, kBlock, 0, stream>>>(args, h.d_chunk_nodes + off, count,
-                                                                              h.d_inv, stride, 0, h.d_chunk_pos + off);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)((threads + kBlock - 1) / kBlock));
+        cfg.blockDim = dim3(kBlock);
+        cfg.stream = stream;
+        cfg.attrs = attr;
+        cfg.numAttrs = (h.pdl_levels && !first) ? 1 : 0;
+        cudaError_t e = cudaLaunchKernelEx(&cfg, k_sweep_cached_level<D, P, double, true>, args,
+                                           (const int*)(h.d_chunk_nodes + off), count, (const double*)h.d_inv, stride,
+                                           0LL, (const int*)(h.d_chunk_pos + off));
+        if (e != cudaSuccess) return e;
+        first = false;
     }
     return cudaGetLastError();
 }

@@ -205,6 +205,10 @@ class InverseAdvectionOperator:
         """1: the fused sweep's level launches overlap (programmatic dependent launch); 0: plain order."""
         check(_lib.lib().allium_sweep_set_fused_pdl(self.h, int(on)), self.h)
 
+    def SetLevelPDL(self, on):
+        """1: the stored-inverse sweep's level launches overlap (programmatic dependent launch); 0: plain order."""
+        check(_lib.lib().allium_sweep_set_level_pdl(self.h, int(on)), self.h)
+
     def IsotropicSource(self, sigma_s, phi, q_iso=None, out=None, out_hi=None, out_lo=None):
         """Per-cell source (sigma_s M phi)/sum(w) + q_iso in FP64, written as float32
         (out) and/or double-float (out_hi, out_lo).  sigma_s [G, Ne] numpy or
