@@ -106,10 +106,6 @@ cudaError_t sweep_chunk(Handle& h, const SweepArgs<double>& args, int c, cudaStr
     const int kBlock = h.block64;
     const long long stride = (long long)h.G * h.ne * h.Nw;
     const int* offs = h.h_chunk_offsets.data() + (size_t)c * (h.num_levels + 1);
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    bool first = true;
     for (int l = 0; l < h.num_levels; ++l) {
         const int off = offs[l];
         const int count = offs[l + 1] - off;
@@ -120,13 +116,14 @@ cudaError_t sweep_chunk(Handle& h, const SweepArgs<double>& args, int c, cudaStr
         cfg.gridDim = dim3((unsigned)((threads + kBlock - 1) / kBlock));
         cfg.blockDim = dim3(kBlock);
         cfg.stream = stream;
-        cfg.attrs = attr;
-        cfg.numAttrs = (h.pdl_levels && !first) ? 1 : 0;
+        // no programmatic dependent launch here: the chunks' level chains run on
+        // several compute streams at once, and blocks waiting early would hold SM
+        // slots that another chain's ready level could use (the one run with it
+        // had a median host-buffer call of 23.6 ms, the runs without 22.0-22.2)
         cudaError_t e = cudaLaunchKernelEx(&cfg, k_sweep_cached_level<D, P, double, true>, args,
                                            (const int*)(h.d_chunk_nodes + off), count, (const double*)h.d_inv, stride,
                                            0LL, (const int*)(h.d_chunk_pos + off));
         if (e != cudaSuccess) return e;
-        first = false;
     }
     return cudaGetLastError();
 }
