@@ -14,11 +14,14 @@ using allium::Handle;
 
 namespace {
 
+// cudaErrorNotSupported from the library's own launchers means an unsupported
+// option or shape (no kernel was launched), the rest a CUDA failure
 #define CUDA_OR_FAIL(h, x)                                   \
     do {                                                     \
         cudaError_t _e = (x);                                \
         if (_e != cudaSuccess) {                             \
             (h).last_error = std::string(#x) + ": " + cudaGetErrorString(_e); \
+            if (_e == cudaErrorNotSupported) return ALLIUM_ERR_UNSUPPORTED; \
             return ALLIUM_ERR_CUDA;                          \
         }                                                    \
     } while (0)

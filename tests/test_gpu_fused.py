@@ -55,9 +55,12 @@ def setup(case, seed=5, tau=None):
     return L, o
 
 
-@pytest.mark.parametrize("case", CASES, ids=IDS)
+@pytest.mark.parametrize("case", CASES + [CASES[6] + ("td",), CASES[3] + ("td",)],
+                         ids=IDS + [IDS[6] + "-td", IDS[3] + "-td"])
 def test_fused_sweep_matches_oracle(case):
-    L, o = setup(case)
+    # "td": with a time absorption tau M_t (per-unit tables carry M_t)
+    td = len(case) > 6
+    L, o = setup(case[:6], tau=2.5 if td else None)
     rng = np.random.default_rng(3)
     nd = L.G * L.ndof
     iso = rng.uniform(0.0, 1.0, nd)
