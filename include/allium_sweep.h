@@ -338,16 +338,15 @@ int allium_sweep_fused_levels(allium_sweep* s, int* num_levels, int* unit_levels
 
 /* Launch overlap of the fused sweep's level launches (no reference
  * counterpart): 1 (default) lets each level's blocks start while the previous
- * level drains (programmatic dependent launch; they load their records, cell
+ * level drains (programmatic dependent launch; they load their records, unit
  * tables and sources, then wait before reading upwind traces), 0 plain
  * stream order.  Results do not depend on it. */
 int allium_sweep_set_fused_pdl(allium_sweep* s, int on);
 
 /* The same for the FP64 (and RIGHT-layout FP32) sweep from stored local
- * inverses (no reference counterpart): 1 (default) lets each level's blocks
- * read their node records and face data and prefetch their stored inverses
- * while the previous level drains, 0 plain stream order.  Results do not
- * depend on it. */
+ * inverses on device vectors (no reference counterpart): 1 (default) lets each
+ * level's blocks read their node records and face data while the previous
+ * level drains, 0 plain stream order.  Results do not depend on it. */
 int allium_sweep_set_level_pdl(allium_sweep* s, int on);
 
 /* r = q + D^T S phi - L psi for a double-float psi: AdvectionOperator::Mult
