@@ -153,18 +153,53 @@ def group_problems(problems):
     return [idx for _, idx in sorted(keys.items())]
 
 
-def solve_batched(problems, method="si", tol=1e-8):
-    """Build one union handle per (order, S_N) group and solve every group."""
+def solve_batched(problems, method="si", tol=1e-8, workers=1):
+    """Build one union handle per (order, S_N) group and solve every group.
+
+    workers > 1 builds and solves that many groups at a time, each on its own
+    CUDA stream from its own host thread: a group's handle, DSA and Krylov
+    vectors live on the stream that was current when the group was built, and
+    the level launches of a small group leave most of the GPU idle, so
+    concurrent groups fill it."""
     t0 = time.perf_counter()
-    groups = [ProblemGroup([problems[i] for i in idx]) for idx in group_problems(problems)]
+    idx = group_problems(problems)
+    streams = [torch.cuda.Stream() for _ in idx] if workers > 1 else [torch.cuda.current_stream() for _ in idx]
+
+    def build(k):
+        with torch.cuda.stream(streams[k]):
+            g = ProblemGroup([problems[j] for j in idx[k]])
+        g.stream = streams[k]
+        return g
+
+    if workers > 1:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            groups = list(ex.map(build, range(len(idx))))
+    else:
+        groups = [build(k) for k in range(len(idx))]
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     res = BatchResult(0.0, t1 - t0, len(groups), len(problems), sum(g.entries for g in groups))
-    for g in groups:
-        if method == "si":
-            g.phi, it, conv = g.solve_si(tol=tol)
-        else:
-            g.phi, it, _, conv = g.solve_ir(tol=tol)
+
+    def run(g):
+        with torch.cuda.stream(g.stream):
+            if method == "si":
+                g.phi, it, conv = g.solve_si(tol=tol)
+            else:
+                g.phi, it, _, conv = g.solve_ir(tol=tol)
+            g.stream.synchronize()
+        return it, conv
+
+    if workers > 1:
+        from concurrent.futures import ThreadPoolExecutor
+        # largest groups first, so that the small ones fill in around them
+        order = sorted(range(len(groups)), key=lambda k: -groups[k].entries)
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            futs = {k: ex.submit(run, groups[k]) for k in order}
+            results = [futs[k].result() for k in range(len(groups))]
+    else:
+        results = [run(g) for g in groups]
+    for g, (it, conv) in zip(groups, results):
         res.iterations.append(it)
         res.converged = res.converged and conv
         res.sweeps64 += g.op.sweeps64

@@ -473,21 +473,25 @@ def batch_section(count):
     """Batched uneven problems: `count` independent one-group 2D problems
     (side U{16..256}, p U{1,2,3}, S4..S12, sigma_t 10^U[-1, log10 50] per cell,
     c U[0.3, 0.99], q = 1, vacuum), each to a 1e-8 relative residual: one union
-    handle per (order, S_N) group solved by FP32-inner / FP64-outer refinement
-    with DSA-preconditioned GMRES, against the same method on one handle per
+    handle per (order, S_N) group, four groups built and solved at a time on
+    their own streams, by FP32-inner / FP64-outer refinement with
+    DSA-preconditioned GMRES, against the same method on one handle per
     problem."""
+    import gc
     import torch
     from allium_gb300.batch import ProblemGroup, random_problems, solve_batched
     probs = random_problems(count, seed=SEED + 7)
     warm = random_problems(6, seed=1, sides=(8, 16))
-    solve_batched(warm, "ir")
+    solve_batched(warm, "ir", workers=4)
     out = {"problems": count, "entries": int(sum(p.mesh.num_elements * (p.order + 1) ** 2 * (p.sn * (p.sn + 2) // 2)
                                               for p in probs))}
-    res, groups = solve_batched(probs, method="ir", tol=1e-8)
+    res, groups = solve_batched(probs, method="ir", tol=1e-8, workers=4)
     out["batched_ir"] = {"seconds": res.seconds, "setup_seconds": res.setup_seconds, "groups": res.groups,
+                         "concurrent_groups": 4,
                          "outer_per_group": res.iterations, "converged": res.converged,
                          "fp64_sweeps": res.sweeps64, "fp32_sweeps": res.sweeps32}
     del groups
+    gc.collect()
     torch.cuda.empty_cache()
     setup = solve = 0.0
     conv = True

@@ -50,3 +50,15 @@ def test_batched_solves_match_single_solves(method):
             a, b = g.dof_off[k], g.dof_off[k + 1]
             err = torch.max(torch.abs(phi[a:b] - ref)).item() / torch.max(torch.abs(ref)).item()
             assert err < 1e-6
+
+
+def test_concurrent_groups_match_sequential_groups():
+    # four groups built and solved at a time, each on its own stream from its own
+    # host thread: the same iterations and answers as one group after another
+    probs = random_problems(12, seed=6, sides=(8, 24))
+    seq, g1 = solve_batched(probs, method="ir", tol=1e-9, workers=1)
+    con, g4 = solve_batched(probs, method="ir", tol=1e-9, workers=4)
+    assert seq.converged and con.converged and seq.iterations == con.iterations
+    for a, b in zip(g1, g4):
+        err = torch.max(torch.abs(a.phi - b.phi)).item() / torch.max(torch.abs(a.phi)).item()
+        assert err < 1e-9
