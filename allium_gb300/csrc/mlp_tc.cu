@@ -24,6 +24,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "allium_sweep.h"
@@ -239,13 +240,17 @@ __global__ void k_transpose_bf16(int rows, int cols, const __nv_bfloat16* __rest
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    // the driver entry point is process-wide; a race here only repeats the lookup
+    static std::atomic<PFN_cuTensorMapEncodeTiled_v12000> cached{nullptr};
+    PFN_cuTensorMapEncodeTiled_v12000 fn = cached.load();
     if (!fn) {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
+            q == cudaDriverEntryPointSuccess) {
             fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+            cached.store(fn);
+        }
     }
     return fn;
 }
@@ -288,14 +293,18 @@ int allium_mlp_gemm_tc(int M, int N, int K, const void* A, long long lda, const 
     g.C = C; g.ldc = ldc; g.Cb = static_cast<__nv_bfloat16*>(C_bf16); g.ldcb = ldcb;
     g.bias = bias; g.alpha = alpha; g.beta = beta; g.relu = relu; g.ksplit = ksplit;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    static bool attr = false;
-    if (!attr) {
+    // the dynamic shared-memory opt-in is a per-device function attribute
+    static std::atomic<unsigned long long> attr_done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return ALLIUM_ERR_CUDA;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
         if (cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  TcShape<128>::SMEM_BYTES) != cudaSuccess ||
             cudaFuncSetAttribute(k_gemm_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  TcShape<256>::SMEM_BYTES) != cudaSuccess)
             return ALLIUM_ERR_CUDA;
-        attr = true;
+        attr_done.fetch_or(bit);
     }
     if (ksplit > 1 &&
         cudaMemset2DAsync(C, (size_t)ldc * sizeof(float), 0, (size_t)N * sizeof(float), (size_t)M, st) != cudaSuccess)

@@ -200,8 +200,13 @@ def gmres(apply, b, x0=None, tol=1e-8, restart=30, maxiter=2000, atol=0.0, prec=
             w -= torch.mv(V[: k + 1].t(), h)
             h2 = dots(V[: k + 1], w)
             w -= torch.mv(V[: k + 1].t(), h2)
-            hk = (h + h2).cpu().numpy()
-            hn = norm(w)
+            if reduce is None:
+                # the Hessenberg column and ||w||^2 in one device-to-host copy
+                col = torch.cat([h + h2, torch.dot(w, w).reshape(1)]).cpu().numpy()
+                hk, hn = col[:-1], math.sqrt(max(float(col[-1]), 0.0))
+            else:
+                hk = (h + h2).cpu().numpy()
+                hn = norm(w)
             H[: k + 1, k] = hk
             H[k + 1, k] = hn
             for i in range(k):

@@ -514,7 +514,8 @@ int allium_mlp_gemm_tc(int M, int N, int K, const void* A, long long lda, const 
 int allium_mlp_transpose_bf16(int rows, int cols, const void* in, long long ldi, void* out, long long ldo, void* stream);
 
 /* Synchronizes the stream; ALLIUM_ERR_TIMEOUT (and the word cleared) if a
- * bounded wait inside allium_mlp_gemm_tc gave up since the last call. */
+ * bounded wait inside allium_mlp_gemm_tc gave up since the last call.  The
+ * word is one per process and device, shared by every stream and thread. */
 int allium_mlp_status(void* stream);
 
 /* dz = dy where y > 0, else 0 (ReLU gradient); dz and/or its BF16 copy. */
