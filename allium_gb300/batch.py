@@ -156,11 +156,12 @@ def group_problems(problems):
 def solve_batched(problems, method="si", tol=1e-8, workers=1):
     """Build one union handle per (order, S_N) group and solve every group.
 
-    workers > 1 builds and solves that many groups at a time, each on its own
-    CUDA stream from its own host thread: a group's handle, DSA and Krylov
-    vectors live on the stream that was current when the group was built, and
-    the level launches of a small group leave most of the GPU idle, so
-    concurrent groups fill it."""
+    workers > 1 solves that many groups at a time, each on its own CUDA stream
+    from its own host thread: a group's handle, DSA and Krylov vectors live on
+    the stream that was current when the group was built, and the level launches
+    of a small group leave most of the GPU idle, so concurrent groups fill it.
+    The groups are built one after another (their setup holds the GIL for most
+    of its host work, and one at a time keeps the peak memory down)."""
     t0 = time.perf_counter()
     idx = group_problems(problems)
     streams = [torch.cuda.Stream() for _ in idx] if workers > 1 else [torch.cuda.current_stream() for _ in idx]
@@ -171,12 +172,7 @@ def solve_batched(problems, method="si", tol=1e-8, workers=1):
         g.stream = streams[k]
         return g
 
-    if workers > 1:
-        from concurrent.futures import ThreadPoolExecutor
-        with ThreadPoolExecutor(max_workers=workers) as ex:
-            groups = list(ex.map(build, range(len(idx))))
-    else:
-        groups = [build(k) for k in range(len(idx))]
+    groups = [build(k) for k in range(len(idx))]   # one at a time: lower peak memory
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     res = BatchResult(0.0, t1 - t0, len(groups), len(problems), sum(g.entries for g in groups))

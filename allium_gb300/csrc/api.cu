@@ -4,6 +4,7 @@
 #include <initializer_list>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -308,11 +309,12 @@ static bool misaligned(const void* a, const void* b, bool da, bool db) {
 
 // Allocate the FP64 factor cache when enabled, supported and it leaves at
 // least half of the free device memory untouched; otherwise sweep without it.
-// Allocate the FP64 factor cache when enabled, supported and it leaves at
-// least half of the free device memory untouched; otherwise sweep without it.
+// The check and the allocation hold a process-wide lock (allium::cache_lock),
+// so handles used from several threads at once decide one after another.
 static void prepare_factor_cache(Handle& h) {
     if (h.d_inv || h.factor_cache == 0 || !allium::factor_cache_supported(h)) return;
     const size_t need = (size_t)h.G * h.ne * h.Nw * h.n * h.n * sizeof(double);
+    std::lock_guard<std::mutex> lock(allium::cache_lock());
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); return; }
     if (need > free_b / 2) return;

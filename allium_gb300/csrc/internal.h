@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "../../include/allium_sweep.h"
@@ -206,6 +207,10 @@ inline void drop_graphs(Handle& h) {
     }
     drop_fused_graphs(h);
 }
+
+// process-wide lock around the optional caches' "fits in half the free
+// memory" decisions (the FP64 factor cache and its FP32 copy)
+std::mutex& cache_lock();
 
 // kernel error bits (d_status)
 constexpr int kErrSingular = 1;

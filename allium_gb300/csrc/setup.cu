@@ -11,6 +11,11 @@
 
 namespace allium {
 
+std::mutex& cache_lock() {
+    static std::mutex m;
+    return m;
+}
+
 // ------------------------------------------------------------ host tables
 namespace {
 

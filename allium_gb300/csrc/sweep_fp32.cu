@@ -64,6 +64,7 @@ static bool ensure_f32_inverses(Handle& h) {
     const int NN = h.n * h.n;
     const long long total = (long long)h.G * h.ne * h.Nw;
     if (!h.f_inv_nodes) {
+        std::lock_guard<std::mutex> lock(cache_lock());
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
         const size_t need = (size_t)total * NN * sizeof(float);

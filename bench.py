@@ -889,6 +889,13 @@ def run_gpu(args):
         line["learned_iterate"] = learned_section(args.trt_steps, min(50, args.trt_steps // 4))
         line["mlp_gemm"] = gemm_section()
         if args.batch_problems > 0:
+            # the 64^3 handle (stored inverses, FP32 copies, fused tables) is not
+            # needed any more: release it before the batched problems' handles
+            del L, srcs, psi
+            import gc
+            gc.collect()
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
             line["batched_uneven"] = batch_section(args.batch_problems)
     if not args.no_cpu and tuple(cells) == CELLS:
         rates, size = cpu_sweep_sample(os.cpu_count() or 1, 3, 1)
