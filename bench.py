@@ -825,7 +825,8 @@ def run_gpu(args):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
                     "ms_per_step": e2e_s * 1e3,
                     "call_ms": {"median": 1e3 * float(np.median(call_s)), "min": 1e3 * min(call_s),
-                                "max": 1e3 * max(call_s)},
+                                "p90": 1e3 * float(np.percentile(call_s, 90)), "max": 1e3 * max(call_s),
+                                "slow_calls_over_1p5x_median": int(sum(c > 1.5 * np.median(call_s) for c in call_s))},
                     "pipeline": {"chunks": pipe["best"]["chunks"], "compute_streams": pipe["best"]["streams"],
                                  "taper": pipe["best"]["taper"],
                                  "trials_ms": {f"{t['chunks']}x{t['streams']}t{t['taper']}": round(t["ms"], 2)
