@@ -649,7 +649,7 @@ int allium_sweep_isotropic_source(allium_sweep* s, const double* sigma_s, const 
 
 int allium_sweep_fused_mult_f32(allium_sweep* s, const float* iso, const float* source, float* psi, double* phi,
                                 int phi_mode, float* psi_hi, float* psi_lo) {
-    if (!s || !psi || phi_mode < 0 || phi_mode > 2 || (phi_mode && !phi) || (!psi_hi != !psi_lo)) return ALLIUM_ERR_ARG;
+    if (!s || !psi || phi_mode < 0 || phi_mode > 3 || (phi_mode && !phi) || (!psi_hi != !psi_lo)) return ALLIUM_ERR_ARG;
     Handle& h = s->h;
     if (int st = fused_check(h, "allium_sweep_fused_mult_f32")) return st;
     if (int st = device_only(h, {iso, source, psi, phi, psi_hi, psi_lo}, "allium_sweep_fused_mult_f32")) return st;

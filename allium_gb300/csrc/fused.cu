@@ -1071,6 +1071,29 @@ __global__ void k_moments_f32(int ne, int Nw, int G, int N, const float2* __rest
     phi[t] = add ? phi[t] + v : v;
 }
 
+// The same sum in plain FP32 (about 1e-6 relative), for the inner operator of
+// a Krylov solve whose own tolerance is far looser: one FMA per angle instead
+// of an error-free product and a TwoSum.
+__global__ void k_moments_f32_fast(int ne, int Nw, int G, int N, const float* __restrict__ w,
+                                   const float* __restrict__ psi, double* __restrict__ phi) {
+    griddep_wait();
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long ndof = (long long)ne * N;
+    if (t >= (long long)G * ndof) return;
+    const int g = (int)(t / ndof);
+    const long long s = t % ndof;
+    const int e = (int)(s / N), i = (int)(s % N);
+    const float* p = psi + fused_index(ne, Nw, N, g, e, 0) + i;
+    float acc0 = 0.f, acc1 = 0.f;   // two chains: half the dependent-FMA latency
+    int a = 0;
+    for (; a + 1 < Nw; a += 2) {
+        acc0 = fmaf(w[a], __ldcg(p + (long long)a * N), acc0);
+        acc1 = fmaf(w[a + 1], __ldcg(p + (long long)(a + 1) * N), acc1);
+    }
+    if (a < Nw) acc0 = fmaf(w[a], __ldcg(p + (long long)a * N), acc0);
+    phi[t] = (double)(acc0 + acc1);
+}
+
 // the same for a double-float psi (DiscreteToMoment::Mult of hi + lo)
 __global__ void k_moments_df(int ne, int Nw, int G, int N, const float2* __restrict__ w, const float* __restrict__ hi,
                              const float* __restrict__ lo, double* __restrict__ phi) {
@@ -1785,8 +1808,12 @@ cudaError_t sweep_body(Handle& h, FusedState& fs, const FusedArgs& a, double* ph
         cfg.stream = st;
         cfg.attrs = attr;
         cfg.numAttrs = pdl ? 1 : 0;
-        FCK(cudaLaunchKernelEx(&cfg, k_moments_f32, h.ne, h.Nw, h.G, h.n, (const float2*)fs.dw, (const float*)a.psi, phi,
-                               phi_mode == 2 ? 1 : 0));
+        if (phi_mode == 3)
+            FCK(cudaLaunchKernelEx(&cfg, k_moments_f32_fast, h.ne, h.Nw, h.G, h.n, (const float*)fs.w,
+                                   (const float*)a.psi, phi));
+        else
+            FCK(cudaLaunchKernelEx(&cfg, k_moments_f32, h.ne, h.Nw, h.G, h.n, (const float2*)fs.dw,
+                                   (const float*)a.psi, phi, phi_mode == 2 ? 1 : 0));
     }
     return cudaGetLastError();
 }

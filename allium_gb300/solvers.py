@@ -312,8 +312,9 @@ class FusedSchur:
         self.sweeps32 = 0
 
     def apply32(self, x, out):
+        # the inner GMRES's operator: moments summed in FP32 (phi_mode 3)
         self.L.IsotropicSource(self.sigma_s, x, None, out=self.iso)
-        self.L.FusedMultF32(self.iso, None, self.psi32, phi=self.tmp, phi_mode=1)
+        self.L.FusedMultF32(self.iso, None, self.psi32, phi=self.tmp, phi_mode=3)
         self.sweeps32 += 1
         torch.sub(x, self.tmp, out=out)
         return out
@@ -377,7 +378,9 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     # rho_0 = D L^{-1} q (the residual of psi = 0)
     if q_iso is not None:
         L.IsotropicSource(None, None, q_iso, out=fs.iso)
-    L.FusedMultF32(fs.iso if q_iso is not None else None, q_hi, fs.psi32, phi=rho, phi_mode=1)
+    # right-hand sides and projections need only FP32 moments (phi_mode 3); the
+    # corrections of phi (phi_mode 1 below) are summed in double-float
+    L.FusedMultF32(fs.iso if q_iso is not None else None, q_hi, fs.psi32, phi=rho, phi_mode=3)
     fs.sweeps32 += 1
     r0 = torch.linalg.norm(rho).item()
     hist, outer, inner_total, conv, residuals, updates = [], 0, 0, False, 0, 0
@@ -414,7 +417,7 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
             L.TransportResidualUpdateF32(fs.iso, fs.psi32, r32)
             updates += 1
         # rho = D L^{-1} r
-        L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=1)
+        L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=3)
         fs.sweeps32 += 1
         outer += 1
     torch.cuda.synchronize()

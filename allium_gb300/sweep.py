@@ -180,7 +180,8 @@ class InverseAdvectionOperator:
     # psi-sized vectors in the fused layout v[((g*Ne + e)*Nw + a)*n + i])
     def FusedMultF32(self, iso, source, psi, phi=None, phi_mode=0, acc=None):
         """psi = L^{-1} (iso + source) in FP32 with phi = D psi (phi_mode 1) or
-        phi += D psi (2) in the same graph; acc = (hi, lo) double-float
+        phi += D psi (2) in the same graph, summed in double-float, or phi = D psi
+        summed in FP32 (3, for inner operators); acc = (hi, lo) double-float
         accumulator that psi is added to.  iso [G*Ndof] float32 per-cell source
         or None, source psi-sized float32 or None."""
         nd = self.G * self.ndof

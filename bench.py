@@ -756,6 +756,7 @@ def run_gpu(args):
     L.synchronize()
     ms_fused = _timed(stream, args.steps, lambda i: L.FusedMultF32(iso, None, fz_psi, phi=fz_phi, phi_mode=1))
     ms_fused_nophi = _timed(stream, args.steps, lambda i: L.FusedMultF32(iso, None, fz_psi))
+    ms_fused_phi32 = _timed(stream, args.steps, lambda i: L.FusedMultF32(iso, None, fz_psi, phi=fz_phi, phi_mode=3))
     # accuracy of the fused sweep on the headline source against the FP64 sweep
     fz_src = torch.empty(N, dtype=torch.float32, device="cuda")
     L.ToFusedLayout(srcs[0], fz_src)
@@ -866,7 +867,8 @@ def run_gpu(args):
                            "note": "node-major layout (the refinement's inner sweep), from an FP32 copy of the stored inverses"},
             "fp32_fused": {
                 "value": N / (ms_fused * 1e-3), "unit": UNIT, "ms_per_step": ms_fused,
-                "ms_without_moments": ms_fused_nophi, "max_rel_err_vs_fp64": err_fused,
+                "ms_without_moments": ms_fused_nophi, "ms_fp32_moments": ms_fused_phi32,
+                "max_rel_err_vs_fp64": err_fused,
                 "levels": fused_levels[0], "unit_levels": bool(fused_levels[1]), "setup_seconds": fused_setup_s,
                 "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
                              "algorithmic_bytes_per_entry": 8,

@@ -321,7 +321,8 @@ int allium_sweep_isotropic_source(allium_sweep* s, const double* sigma_s, const 
  * NULL) plus an optional psi-sized FP32 source, followed by
  * DiscreteToMoment::Mult (src/transport_op.cpp:3-31) of the FP32 psi summed in
  * double-float arithmetic: phi_mode 0 leaves phi alone, 1 writes phi = D psi,
- * 2 adds D psi to phi (FP64).  psi receives the FP32 angular flux;
+ * 2 adds D psi to phi (FP64); 3 writes phi = D psi summed in plain FP32 (about
+ * 1e-6 relative, for the inner operator of a Krylov solve).  psi receives the FP32 angular flux;
  * psi_hi/psi_lo (or NULL) is a double-float vector that psi is added to.
  * source may equal psi. */
 int allium_sweep_fused_mult_f32(allium_sweep* s, const float* iso, const float* source, float* psi, double* phi,

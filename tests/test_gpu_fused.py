@@ -77,6 +77,11 @@ def test_fused_sweep_matches_oracle(case):
     got = right_of_fused(L, psi.cpu().numpy().astype(np.float64))
     assert rel_err(got, ref) < TOL32
     assert rel_err(phi.cpu().numpy(), phi_ref) < TOL32
+    # the moments summed in plain FP32 (phi_mode 3, the inner operator's)
+    phi3 = torch.full((nd,), 7.0, dtype=torch.float64, device="cuda")
+    L.FusedMultF32(d_iso, d_src, psi, phi=phi3, phi_mode=3)
+    L.synchronize()
+    assert rel_err(phi3.cpu().numpy(), phi_ref) < TOL32
     # the same through the conversion back to RIGHT FP64
     back = torch.empty(L.width, dtype=torch.float64, device="cuda")
     L.FromFusedLayout(psi, None, back)
