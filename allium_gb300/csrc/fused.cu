@@ -244,14 +244,6 @@ template <int NP>
 __device__ __forceinline__ float get(const float2 (&row)[NP], int j) {
     return (j & 1) ? row[j >> 1].y : row[j >> 1].x;
 }
-template <int NP>
-__device__ __forceinline__ void fma_to(float2 (&row)[NP], int j, float a, float b) {
-    if (j & 1) row[j >> 1].y = fmaf(a, b, row[j >> 1].y); else row[j >> 1].x = fmaf(a, b, row[j >> 1].x);
-}
-template <int NP>
-__device__ __forceinline__ void put(float2 (&row)[NP], int j, float v) {
-    if (j & 1) row[j >> 1].y = v; else row[j >> 1].x = v;
-}
 
 template <int N>
 __device__ __forceinline__ void ld_vec(const float* p, float (&r)[N]) {
