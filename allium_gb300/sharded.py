@@ -193,3 +193,33 @@ class AngleShardedGMRES(AngleShardedSI):
         phi, it, hist = gmres(self.apply, b, tol=tol, restart=restart, maxiter=maxiter,
                               reduce=self._reduce if self.ng > 1 else None)
         return phi, it, hist[-1] <= tol
+
+
+class AngleShardedRefinement:
+    """The mixed-precision refinement with no FP64 sweep (solvers.refine_fused)
+    with the directions split over the ranks of `group`.
+
+    Each rank's handle sweeps its slice of the directions in FP32; every moment
+    vector a sweep produces (the right-hand side, each inner GMRES product, the
+    correction of phi, each projection of the residual) is completed by one
+    allreduce, so the GMRES work in moment space is repeated identically on every
+    rank.  The transport residual r = q + D^T S phi - L psi needs no exchange:
+    it is local to each direction once phi is complete.  sigma_s is scaled by
+    the slice's share of the weight sum, as in AngleShardedSI."""
+
+    def __init__(self, mesh, order, quad, sigma_t, sigma_s, rank, world, group=None):
+        from .sweep import InverseAdvectionOperator
+        self.a0, self.a1 = angle_slice(quad.size, rank, world)
+        sub = sub_quadrature(quad, self.a0, self.a1)
+        scale = float(np.sum(sub.weights) / np.sum(quad.weights))
+        self.sigma_s = np.ascontiguousarray(sigma_s, dtype=np.float64) * scale
+        self.L = InverseAdvectionOperator(mesh, order, sub, np.ascontiguousarray(sigma_t, dtype=np.float64))
+        self.group = group
+
+    def solve(self, q_cell, tol=1e-8, inner_tol=1e-4):
+        """Returns the SolveResult of refine_fused; phi is the full scalar flux."""
+        from .solvers import refine_fused
+        from .sweep import FormTransportSource
+        q = torch.from_numpy(FormTransportSource(self.L, np.ascontiguousarray(q_cell, dtype=np.float64))).cuda()
+        return refine_fused(self.L, self.sigma_s, q, tol=tol, inner_tol=inner_tol,
+                            allreduce=lambda t: allreduce_sum(t, self.group))

@@ -301,8 +301,9 @@ class FusedSchur:
     (one launch per wavefront level) and sums D psi (allium_sweep_fused_mult_f32);
     psi stays in a scratch vector of the fused layout."""
 
-    def __init__(self, Linv: InverseAdvectionOperator, sigma_s):
+    def __init__(self, Linv: InverseAdvectionOperator, sigma_s, allreduce=None):
         self.L = Linv
+        self.allreduce = allreduce
         dev = torch.device("cuda")
         self.sigma_s = torch.as_tensor(np.ascontiguousarray(sigma_s, dtype=np.float64).reshape(-1), device=dev)
         self.n = Linv.G * Linv.ndof
@@ -315,6 +316,8 @@ class FusedSchur:
         # the inner GMRES's operator: moments summed in FP32 (phi_mode 3)
         self.L.IsotropicSource(self.sigma_s, x, None, out=self.iso)
         self.L.FusedMultF32(self.iso, None, self.psi32, phi=self.tmp, phi_mode=3)
+        if self.allreduce is not None:
+            self.allreduce(self.tmp)
         self.sweeps32 += 1
         torch.sub(x, self.tmp, out=out)
         return out
@@ -332,7 +335,7 @@ def split_isotropic(Linv: InverseAdvectionOperator, q):
 
 
 def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, tol=1e-8, inner_tol=1e-4, restart=30,
-                 max_outer=20, inner_maxiter=500, prec=None, incremental=None):
+                 max_outer=20, inner_maxiter=500, prec=None, incremental=None, allreduce=None):
     """FP32-inner / FP64-outer refinement on the transport system itself,
     L psi - D^T S D psi = q, with no FP64 sweep.
 
@@ -351,11 +354,19 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     ||rho|| <= tol ||rho_0||.
     q is the psi-sized RIGHT FP64 source (a CUDA tensor) or q_iso its per-cell
     part when it is the same in every direction.  Returns a SolveResult whose
-    phi is the FP64 scalar flux."""
+    phi is the FP64 scalar flux.
+
+    allreduce(t), when given, sums a moment vector over the ranks that hold the
+    other directions (in place): Linv then sweeps one slice of the directions,
+    sigma_s is scaled by the slice's share of the weight sum, and every moment
+    vector the sweeps produce is completed by one allreduce, so the moment-space
+    (GMRES) work is repeated identically on every rank while psi and the
+    residual stay sharded."""
     t0 = time.perf_counter()
     L = Linv
     dev = torch.device("cuda")
-    fs = FusedSchur(L, sigma_s)
+    fs = FusedSchur(L, sigma_s, allreduce)
+    red = allreduce if allreduce is not None else (lambda t: t)
     W, n = L.width, fs.n
     q_rest = None
     if q_iso is None:
@@ -381,6 +392,7 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     # right-hand sides and projections need only FP32 moments (phi_mode 3); the
     # corrections of phi (phi_mode 1 below) are summed in double-float
     L.FusedMultF32(fs.iso if q_iso is not None else None, q_hi, fs.psi32, phi=rho, phi_mode=3)
+    red(rho)
     fs.sweeps32 += 1
     r0 = torch.linalg.norm(rho).item()
     hist, outer, inner_total, conv, residuals, updates = [], 0, 0, False, 0, 0
@@ -404,6 +416,7 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
         # psi += dpsi = L^{-1} (r + D^T S d); phi += D dpsi (double-float sums)
         L.IsotropicSource(fs.sigma_s, d, q_iso if outer == 0 else None, out=fs.iso)
         L.FusedMultF32(fs.iso, q_hi if outer == 0 else r32, fs.psi32, phi=dphi, phi_mode=1, acc=(hi, lo))
+        red(dphi)
         fs.sweeps32 += 1
         phi += dphi
         if outer == 0 or not incremental:
@@ -418,6 +431,7 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
             updates += 1
         # rho = D L^{-1} r
         L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=3)
+        red(rho)
         fs.sweeps32 += 1
         outer += 1
     torch.cuda.synchronize()

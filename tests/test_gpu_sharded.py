@@ -3,7 +3,8 @@ two processes that share one GPU, each sweeping half of the directions
 through GPUBackend, with gloo carrying the moment allreduce through host
 memory (no kernel of one rank waits for the other).  Source iteration and
 GMRES both equal the unsharded GPU solve to 1e-12 relative with the same
-iteration count."""
+iteration count; the sharded mixed-precision refinement (FP32 sweeps, no FP64
+sweep) reaches the FP64 solution to 1e-8."""
 import os
 import socket
 
@@ -69,3 +70,32 @@ def test_two_ranks_share_one_gpu(tmp_path, method):
     for r in rs:
         assert r[-1] == 1.0 and int(r[-2]) == it_ref
         assert np.max(np.abs(r[:-4] - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def _refine_worker(rank, world, port, path):
+    import torch.distributed as dist
+    from allium_gb300.sharded import AngleShardedRefinement
+    torch.cuda.set_device(0)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    mesh, quad, sigma, ss, q = _case()
+    solver = AngleShardedRefinement(mesh, 1, quad, sigma, ss, rank, world)
+    res = solver.solve(q, tol=1e-10)
+    torch.cuda.synchronize()
+    np.save(f"{path}.{rank}.npy", np.concatenate([res.phi.cpu().numpy(), [res.iterations, res.converged]]))
+    dist.destroy_process_group()
+
+
+def test_two_ranks_refinement_without_fp64_sweeps(tmp_path):
+    mp = pytest.importorskip("torch.multiprocessing")
+    ref, _, _ = _unsharded("gmres")
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    path = str(tmp_path / "phi")
+    mp.spawn(_refine_worker, args=(2, port, path), nprocs=2, join=True)
+    rs = [np.load(f"{path}.{r}.npy") for r in range(2)]
+    assert np.array_equal(rs[0], rs[1])   # the moment-space work is the same on both ranks
+    assert rs[0][-1] == 1.0
+    assert np.max(np.abs(rs[0][:-2] - ref)) < 1e-8 * np.max(np.abs(ref))
