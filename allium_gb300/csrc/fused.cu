@@ -111,7 +111,7 @@ constexpr int kFusedWarps = kFusedBlock / 32;
 constexpr int kSweepBlock = 64;
 constexpr int kSweepWarps = kSweepBlock / 32;
 constexpr int kSweepMinBlocks = 10;
-constexpr int kSlots = 4;          // staged cell tables per warp and round (sweep)
+constexpr int kSlots = 4;          // staged tables per warp: units (sweep), cells per round (update)
 constexpr int kSlotsDF = 2;        // staged cell tables per warp and round (residual)
 constexpr int kWaitLimit = 1 << 20;
 constexpr int kMaxUnits = 64;      // units per cell the schedule setup handles
@@ -914,8 +914,8 @@ __global__ void __launch_bounds__(kSweepBlock, kSweepMinBlocks) k_fused_level(Fu
     }
     // the upwind traces were written by earlier levels: after the wait, fold each
     // inflow face's term |Omega.n| F_k u_k into b as its trace arrives, the face
-    // block and normal read from the cell's staged table.  The schedule packs at
-    // most kSlots cells into a warp, so every table of the warp was staged by
+    // block and normal read from the unit's staged table.  The schedule packs at
+    // most kSlots units into a warp, so every table of the warp was staged by
     // stage_runs.
     griddep_wait();
     const bool staged = valid && run < kSlots;
@@ -1697,7 +1697,7 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
         k_level_starts<<<blocks(nlev + 1, 128), 128, 0, h.stream>>>(nlev, keys_out, N, starts);
         step(cudaGetLastError());
     }
-    // warps of at most kSlots cells: runs, their padded positions, level sizes, records
+    // warps of at most kSlots units: runs, their padded positions, level sizes, records
     if (err == cudaSuccess) {
         k_run_flags<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, flag);
         step(cudaGetLastError());
