@@ -494,8 +494,11 @@ __global__ void k_fused_nodes(long long n, int Nw, int dim, const double* __rest
 // (unit_of_node given) or by node e Nw + a.
 // sort key of a node record: (level, unit); units are numbered cell by cell, so
 // a level's records come out grouped by cell, then unit, then (stable) angle
+// key = level (bits 36 and up) | face pattern (bits ubits..35, when ubits < 36) | unit:
+// within a level the units of one face pattern are adjacent, so the units that
+// share a warp fold the same inflow faces (no divergence in the fold)
 __global__ void k_fused_keys(long long n, int Nw, const int2* __restrict__ recs, const int* __restrict__ level_of,
-                             bool unit_levels, const int* __restrict__ unit_of_node,
+                             bool unit_levels, const int* __restrict__ unit_of_node, int ubits,
                              unsigned long long* __restrict__ keys) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -504,7 +507,8 @@ __global__ void k_fused_keys(long long n, int Nw, const int2* __restrict__ recs,
     const long long v = (long long)r.x * Nw + a;
     const int u = unit_of_node[v];
     const int lev = unit_levels ? level_of[u] : level_of[v];
-    keys[t] = ((unsigned long long)lev << 36) | (unsigned long long)(unsigned)u;
+    const unsigned long long pat = ubits < 36 ? (unsigned long long)((unsigned)r.y >> 16) << ubits : 0ull;
+    keys[t] = ((unsigned long long)lev << 36) | pat | (unsigned long long)(unsigned)u;
 }
 
 // cell and face pattern of every unit (all nodes of a unit share both)
@@ -707,15 +711,15 @@ __global__ void k_pack_fill(long long n, int2* __restrict__ out, int* __restrict
 __global__ void k_pack_scatter(long long n, const unsigned long long* __restrict__ keys, const int2* __restrict__ recs,
                                const int* __restrict__ ridx, const int* __restrict__ flag,
                                const int* __restrict__ run_start, const int* __restrict__ run_pos,
-                               const long long* __restrict__ out_starts, int2* __restrict__ out,
-                               int* __restrict__ out_unit) {
+                               const long long* __restrict__ out_starts, unsigned long long umask,
+                               int2* __restrict__ out, int* __restrict__ out_unit) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int r = ridx[i] + flag[i] - 1;   // run of record i (inclusive scan - 1)
     const int l = (int)(keys[i] >> 36);
     const long long o = out_starts[l] + run_pos[r] + (i - run_start[r]);
     out[o] = recs[i];
-    out_unit[o] = (int)(keys[i] & 0xFFFFFFFFull);
+    out_unit[o] = (int)(keys[i] & umask);
 }
 
 __global__ void k_fused_cells(int ne, int dim, int p, int nf, const Slot* __restrict__ slots,
@@ -1130,9 +1134,11 @@ struct ResidArgs {
 // Face terms first (each face's trace loaded where it is used), then the
 // volume part y += (sum_d Omega_d G_d + sigma M [+ tau Mt]) psi over the
 // columns j: a column's matrix entries are combined with Omega, sigma, tau and
-// multiplied by psi_j for two rows per packed operation.
+// multiplied by psi_j for two rows per packed operation.  Five 128-thread
+// blocks per SM (96 registers, a few spilled) run the 64^3 S12 residual in
+// 8.7 ms against 10.0 ms at four blocks (118 registers, no spills).
 template <int D, int P, bool TD>
-__global__ void __launch_bounds__(kFusedBlock, 4) k_residual_df(ResidArgs f) {
+__global__ void __launch_bounds__(kFusedBlock, 5) k_residual_df(ResidArgs f) {
     using S = Shape<D, P>;
     using T = DTab<D, P, TD>;
     constexpr int N = S::N, NF = S::NF, NFACE = S::NFACE;
@@ -1620,9 +1626,9 @@ cudaError_t unit_levels(Handle& h, int** unit_of_node, int** level_of_unit, int*
 
 // Node records, cell neighbour data and FP32 angles: geometry only, built once.
 // Levels are the unit levels when the unit graph allows (else the node levels);
-// within each level the records are ordered (cell, face pattern, angle): a
-// cell's angles in the level are adjacent, so a warp spans few cells (one table
-// copy each) and the angles of one face pattern stay together.
+// within each level the records are ordered (face pattern, cell, angle): a
+// unit's angles are adjacent, so a warp spans few units (one table copy each),
+// and the units of a warp fold the same inflow faces.
 cudaError_t prepare_common(Handle& h, FusedState& fs) {
     if (fs.nodes) return cudaSuccess;
     const long long N = (long long)h.ne * h.Nw;
@@ -1651,6 +1657,9 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     int lev_bits = 1;
     while ((1 << lev_bits) < nlev + 1) ++lev_bits;
     const int end_bit = 36 + lev_bits;
+    // the face pattern (at most 12 bits) sits between the level and the unit
+    // when the unit ids fit in 24 bits
+    const int ubits = nunits <= (1 << 24) ? 24 : 36;
     std::vector<long long> hs(nlev + 1);
     auto step = [&](cudaError_t e) { if (err == cudaSuccess) err = e; };
     int2* sorted = nullptr;
@@ -1677,7 +1686,8 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     step(cudaMalloc(&starts, (nlev + 1) * sizeof(long long)));
     if (err == cudaSuccess) {
         k_fused_nodes<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, h.dim, h.d_dots, h.d_slots, recs);
-        k_fused_keys<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, recs, level_of, fs.unit_levels, unit, keys);
+        k_fused_keys<<<blocks(N, 256), 256, 0, h.stream>>>(N, h.Nw, recs, level_of, fs.unit_levels, unit, ubits,
+                                                          keys);
         step(cudaGetLastError());
     }
     step(cudaMalloc(&fs.unit_cell, (size_t)nunits * sizeof(int)));
@@ -1733,7 +1743,7 @@ cudaError_t prepare_common(Handle& h, FusedState& fs) {
     if (err == cudaSuccess) {
         k_pack_fill<<<blocks(ps[nlev], 256), 256, 0, h.stream>>>(ps[nlev], fs.nodes, fs.rec_unit);
         k_pack_scatter<<<blocks(N, 256), 256, 0, h.stream>>>(N, keys_out, sorted, ridx, flag, run_start, run_pos,
-                                                             pstart, fs.nodes, fs.rec_unit);
+                                                             pstart, (1ull << ubits) - 1, fs.nodes, fs.rec_unit);
         step(cudaGetLastError());
     }
     if (err == cudaSuccess) step(cudaStreamSynchronize(h.stream));
