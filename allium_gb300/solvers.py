@@ -328,9 +328,9 @@ def split_isotropic(Linv: InverseAdvectionOperator, q):
     same in every direction (FormTransportSource of an isotropic density with
     vacuum boundaries), else (None, q)."""
     v = q.view(Linv.G, Linv.Nw, Linv.ndof)
-    q0 = v[:, :1, :]
-    if bool(torch.all(v == q0).item()):
-        return q0.reshape(-1).contiguous(), None
+    lo, hi = torch.aminmax(v, dim=1)   # one pass over q, no psi-sized temporary
+    if torch.equal(lo, hi):
+        return v[:, 0, :].reshape(-1).contiguous(), None
     return None, q
 
 
@@ -348,9 +348,11 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     corrects psi += L^{-1} (r + D^T S d) with one more FP32 sweep, whose graph
     also sums D of the correction (double-float sums) into phi.  The first
     residual is evaluated in double-float; later ones (incremental, the default
-    for tol >= 1e-10) are updated in FP32 from the previous one,
-    r += D^T S D dpsi - L dpsi, which is accurate to ~1e-7 of the previous
-    residual because the correction dpsi is small.  Stops when
+    for tol >= 1e-10) take a closed form: the correction sweep solved
+    L dpsi = r + D^T S d, so the new residual r + D^T S D dpsi - L dpsi is
+    D^T S (dphi - d), exact up to the FP32 solve error of dpsi (the same order
+    as an FP32 evaluation of L dpsi, ~1e-7 of the correction), and per cell:
+    the sweeps after it read no psi-sized source.  Stops when
     ||rho|| <= tol ||rho_0||.
     q is the psi-sized RIGHT FP64 source (a CUDA tensor) or q_iso its per-cell
     part when it is the same in every direction.  Returns a SolveResult whose
@@ -396,6 +398,7 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
     fs.sweeps32 += 1
     r0 = torch.linalg.norm(rho).item()
     hist, outer, inner_total, conv, residuals, updates = [], 0, 0, False, 0, 0
+    r_cell = None   # m with r = D^T S m when the residual is per cell, else r is in r32
     if r0 == 0.0:
         res = SolveResult(phi, 0, True, [0.0], time.perf_counter() - t0, 0, fs.sweeps32)
         res.inner_iterations, res.residuals_df, res.residual_updates = 0, 0, 0
@@ -414,23 +417,35 @@ def refine_fused(Linv: InverseAdvectionOperator, sigma_s, q=None, q_iso=None, to
                          final_residual=False)
         inner_total += it
         # psi += dpsi = L^{-1} (r + D^T S d); phi += D dpsi (double-float sums)
-        L.IsotropicSource(fs.sigma_s, d, q_iso if outer == 0 else None, out=fs.iso)
-        L.FusedMultF32(fs.iso, q_hi if outer == 0 else r32, fs.psi32, phi=dphi, phi_mode=1, acc=(hi, lo))
+        if outer == 0:
+            L.IsotropicSource(fs.sigma_s, d, q_iso, out=fs.iso)
+            src = q_hi
+        elif r_cell is None:
+            L.IsotropicSource(fs.sigma_s, d, None, out=fs.iso)
+            src = r32
+        else:
+            r_cell += d
+            L.IsotropicSource(fs.sigma_s, r_cell, None, out=fs.iso)
+            src = None
+        L.FusedMultF32(fs.iso, src, fs.psi32, phi=dphi, phi_mode=1, acc=(hi, lo))
         red(dphi)
         fs.sweeps32 += 1
         phi += dphi
+        # the new residual r, then rho = D L^{-1} r
         if outer == 0 or not incremental:
             # r = q + D^T S phi - L psi in double-float arithmetic
             L.IsotropicSource(fs.sigma_s, phi, q_iso, out_hi=iso_hi, out_lo=iso_lo)
             L.TransportResidualDF(iso_hi, iso_lo, hi, lo, r32, q_hi, q_lo)
             residuals += 1
+            r_cell = None
+            L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=3)
         else:
-            # r += D^T S D dpsi - L dpsi in FP32
-            L.IsotropicSource(fs.sigma_s, dphi, None, out=fs.iso)
-            L.TransportResidualUpdateF32(fs.iso, fs.psi32, r32)
+            # the sweep solved L dpsi = r + D^T S d, so the new residual
+            # r + D^T S D dpsi - L dpsi is D^T S (dphi - d): per cell, isotropic
+            r_cell = torch.sub(dphi, d)
             updates += 1
-        # rho = D L^{-1} r
-        L.FusedMultF32(None, r32, fs.psi32, phi=rho, phi_mode=3)
+            L.IsotropicSource(fs.sigma_s, r_cell, None, out=fs.iso)
+            L.FusedMultF32(fs.iso, None, fs.psi32, phi=rho, phi_mode=3)
         red(rho)
         fs.sweeps32 += 1
         outer += 1

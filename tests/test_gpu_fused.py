@@ -222,6 +222,25 @@ def test_refine_fused_reaches_fp64_solution(case):
     assert err < 1e-6
 
 
+@pytest.mark.parametrize("directional", [False, True])
+def test_refine_fused_many_outer_steps(directional):
+    """A loose inner tolerance forces several outer steps, so the per-cell
+    closed-form residual D^T S (dphi - d) is carried through more than one
+    correction (and, with an inflow boundary, follows a psi-sized one)."""
+    from allium_gb300.solvers import SchurOperator, refine_fused, true_residual
+    L, o = setup(CASES[4])
+    rng = np.random.default_rng(21)
+    ne = L.mesh.num_elements
+    sigma_s = L._keep[6] * rng.uniform(0.5, 0.99, (L.G, ne))
+    inflow = np.ones((1, 8)) if directional else None
+    q = torch.from_numpy(FormTransportSource(L, rng.uniform(0.0, 1.0, (L.G, ne)), inflow)).cuda()
+    res = refine_fused(L, sigma_s, q, tol=1e-8, inner_tol=0.2, max_outer=60)
+    assert res.converged and res.sweeps64 == 0
+    assert res.iterations >= 3 and res.residuals_df == 1 and res.residual_updates == res.iterations - 1
+    op = SchurOperator(L, sigma_s)
+    assert true_residual(op, op.rhs(q), res.phi) < 2e-8
+
+
 def test_refine_fused_with_directional_source():
     """An inflow boundary makes q direction dependent: the psi-sized part goes
     through the fused-layout double-float source."""
