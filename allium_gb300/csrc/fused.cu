@@ -106,11 +106,12 @@ struct DTab {
 
 constexpr int kFusedBlock = 128;
 constexpr int kFusedWarps = kFusedBlock / 32;
-// the sweep's level kernel: 64-thread blocks, at most 96 registers (10 blocks
-// per SM); smaller blocks finish a level's last wave sooner
+// the sweep's level kernel: 64-thread blocks, at most 72 registers (14 blocks
+// per SM; 3.14 ms at 64^3 S12 against 3.22 ms at 10 blocks and 96 registers and
+// 3.61 ms at 16 blocks and 64); smaller blocks finish a level's last wave sooner
 constexpr int kSweepBlock = 64;
 constexpr int kSweepWarps = kSweepBlock / 32;
-constexpr int kSweepMinBlocks = 10;
+constexpr int kSweepMinBlocks = 14;
 constexpr int kSlots = 4;          // staged tables per warp: units (sweep), cells per round (update)
 constexpr int kSlotsDF = 2;        // staged cell tables per warp and round (residual)
 constexpr int kWaitLimit = 1 << 20;
