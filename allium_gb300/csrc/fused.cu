@@ -112,7 +112,11 @@ constexpr int kFusedWarps = kFusedBlock / 32;
 constexpr int kSweepBlock = 64;
 constexpr int kSweepWarps = kSweepBlock / 32;
 constexpr int kSweepMinBlocks = 14;
-constexpr int kSlots = 4;          // staged tables per warp: units (sweep), cells per round (update)
+// staged unit tables per warp in the sweep: two (2.84 ms at 64^3 S12) rather than
+// three (3.06) or four (3.11): less shared memory per block leaves more L1 for the
+// record, source and neighbour loads, at the cost of more padding lanes
+constexpr int kSlots = 2;
+constexpr int kSlotsUpdate = 4;    // staged cell tables per warp and round (residual update)
 constexpr int kSlotsDF = 2;        // staged cell tables per warp and round (residual)
 constexpr int kWaitLimit = 1 << 20;
 constexpr int kMaxUnits = 64;      // units per cell the schedule setup handles
@@ -1305,8 +1309,8 @@ __global__ void __launch_bounds__(kFusedBlock) k_residual_update_f32(UpdateArgs 
     using T = Tab<D, P, TD>;
     constexpr int N = S::N, NF = S::NF, NFACE = S::NFACE;
     constexpr int NP = (N + 1) / 2;
-    __shared__ __align__(128) float s_tab[kFusedWarps * kSlots * T::size];
-    __shared__ __align__(8) unsigned long long s_bar[kFusedWarps * kSlots];
+    __shared__ __align__(128) float s_tab[kFusedWarps * kSlotsUpdate * T::size];
+    __shared__ __align__(8) unsigned long long s_bar[kFusedWarps * kSlotsUpdate];
     const int warp = threadIdx.x >> 5;
     const long long total = (long long)f.G * f.ne * f.Nw;
     const long long t = (long long)blockIdx.x * kFusedBlock + threadIdx.x;
@@ -1318,10 +1322,10 @@ __global__ void __launch_bounds__(kFusedBlock) k_residual_update_f32(UpdateArgs 
         e = (int)(rr % f.ne);
         g = (int)(rr / f.ne);
     }
-    float* wtab = s_tab + warp * kSlots * T::size;
-    unsigned long long* wbar = s_bar + warp * kSlots;
+    float* wtab = s_tab + warp * kSlotsUpdate * T::size;
+    unsigned long long* wbar = s_bar + warp * kSlotsUpdate;
     bool start = false;
-    const int run = stage_runs<kSlots>(wtab, wbar, f.tab, T::size, valid, g * f.ne + e, e, start);
+    const int run = stage_runs<kSlotsUpdate>(wtab, wbar, f.tab, T::size, valid, g * f.ne + e, e, start);
     const long long idx = fused_index(f.ne, f.Nw, N, g, e, a);
     float x[N], y[N];
     float4 om = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1333,7 +1337,7 @@ __global__ void __launch_bounds__(kFusedBlock) k_residual_update_f32(UpdateArgs 
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) y[i] = 0.f;
-    for_each_round<kSlots>(wtab, wbar, f.tab, T::size, valid, run, start, e, f.status, [&](unsigned tb) {
+    for_each_round<kSlotsUpdate>(wtab, wbar, f.tab, T::size, valid, run, start, e, f.status, [&](unsigned tb) {
         const float omv[3] = {om.x, om.y, om.z};
         // volume part: row i of (sum_d Omega_d G_d + sigma M [+ tau Mt]) dotted with x
         float2 xp[NP];
