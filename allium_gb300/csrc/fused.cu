@@ -23,8 +23,8 @@
 //
 // k_fused_level work unit: one thread per (cell, angle, group) node of a level.
 // Nodes come from a record {cell, angle | face pattern << 16}, sorted within
-// each level by (cell, unit, angle) and packed so that a warp holds at most
-// kSlots units (padding records {-1, 0} close a warp early).  Each warp copies
+// each level by (face pattern, unit, angle) and packed so that a warp holds at
+// most kSlots units (padding records {-1, 0} close a warp early).  Each warp copies
 // the FP32 tables of its units (B_d = G_d + the unit's outflow-face terms
 // n_{k,d} F_k, M, [Mt], F_k and the outward face normals, 1.5 KB for a
 // trilinear hex) into shared memory with cp.async.bulk and an mbarrier per
